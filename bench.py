@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark of the plain primal-dual solver on the 3-D coupled workload.
+
+Workload (one "step" = one primal-dual iteration over the whole problem):
+  3-D coupled 4-channel Frobenius TGV with KL discrepancy, 256x256 in-plane x 60
+  slices, 256 detector bins x 71 angles in [-70, 70] degrees, mu = (0.2, 5e-4,
+  4e-3, 5e-4), alpha = (4, 1); seeded synthetic ellipsoid phantoms (channel 0
+  dense with Poisson noise at peak 1e4, channels 1-3 sparse at peak 20).
+Metric: voxel-iterations per second (voxel-channels x iterations / s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's algorithm on the host CPU: the oracle
+(oracle/tgv_oracle.c), an FP32 restatement that reproduces the reference's own
+kernels bit for bit (tests/test_oracle_golden.py), on all host threads, each step
+one iteration over a slab of slices sized to keep the run within minutes.
+Multi-GPU: one independent replica per rank (the problems are independent), no
+collective on the data path; the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W = dict(N=256, Nz=60, C=4, nang=71, alpha=(4.0, 1.0), mu=[0.2, 5e-4, 4e-3, 5e-4], peaks=[1e4, 20.0, 20.0, 20.0],
+         stated_iterations=2500)
+METRIC = "voxel-iter/s"
+WORKLOAD_NAME = "3D FROB3D TGV-KL 256x256x60, 4 channels, 256 bins x 71 angles"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(V, Sb):
+    """Bytes one iteration must move (3-D TGV): 172 per voxel-channel + 16 per bin.
+
+    k_dual   reads ubar 4, pbar 12, v 12, w 24; writes v 12, w 24        (88 B/voxel-ch)
+    k_fwd    reads f 4, lambda 4; writes lambda 4, K ubar 4              (16 B/bin; + ubar 4 B/voxel-ch re-read)
+    k_primal reads u 4, p 12, v 12, w 24, lambda 4/bin; writes u, ubar 4+4, p, pbar 12+12 (84 B/voxel-ch)
+    """
+    return {"iteration": 172 * V + 16 * Sb, "k_dual": 88 * V, "k_fwd": 4 * V + 16 * Sb,
+            "k_primal": 84 * V + 4 * Sb}
+
+
+def make_problem_data(seed=0):
+    """Host sinograms [C][nang, Nz, nd] of the seeded phantom, projected on the GPU."""
+    import torch
+
+    from graptor_gb300 import phantom, solver
+    N, Nz, C, nang = W["N"], W["Nz"], W["C"], W["nang"]
+    vol = phantom.ellipsoids_3d(N, Nz, C, 12, seed)  # [c, z, y, x]
+    ang = phantom.angles_deg(nang)
+    S = C * Nz
+    img = torch.from_numpy(vol.reshape(S, N * N).T.copy()).cuda()
+    sino = torch.zeros(nang * N, S, device="cuda")
+    solver.radon(img.data_ptr(), sino.data_ptr(), ang, N, N, S)
+    g = sino.cpu().numpy().T.reshape(C, Nz, nang, N)
+    out = []
+    for c in range(C):
+        noisy = phantom.poisson(g[c], W["peaks"][c], seed + c)  # [z, nang, nd]
+        out.append(np.ascontiguousarray(np.transpose(noisy, (1, 0, 2))))  # [nang, Nz, nd]
+    del img, sino
+    return out, ang
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [v for v in vis.split(",") if v.strip().isdigit()]
+        self.index = int(ids[index]) if index < len(ids) else index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not self.path:
+            return None
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        load = [s for s in sm if s > 0.5 * smax] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": smax, "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(seconds=15.0):
+    """The oracle (reference-exact FP32 port) on all host threads, bounded sample."""
+    from graptor_gb300 import phantom
+    from oracle import oracle as O
+    N, C, nang = W["N"], W["C"], W["nang"]
+    Nz = 8
+    rng = np.random.default_rng(0)
+    ang = phantom.angles_deg(nang)
+    ofs = O.radon_struct(ang, N, N)
+    f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
+    s = O.Solver(3, N, Nz, C, N, ofs, f, W["alpha"], W["mu"], 100.0, O.KL, O.TGV, O.FROB)
+    s.run(1)
+    t0 = time.perf_counter()
+    it = 0
+    while time.perf_counter() - t0 < seconds or it < 2:
+        s.run(1)
+        it += 1
+    dt = time.perf_counter() - t0
+    V = N * N * Nz * C
+    return {"value": V * it / dt, "unit": METRIC, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{it} iterations of the same problem at 256x256x{Nz} slices x 4 channels, 71 angles "
+                      f"(oracle/tgv_oracle.c, OpenMP {os.cpu_count()} threads, {dt:.1f} s)"}
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference algorithm on the host CPU (oracle port), rank 0 only."""
+    if rank != 0:
+        return None
+    from graptor_gb300 import phantom
+    from oracle import oracle as O
+    N, C, nang = W["N"], W["C"], W["nang"]
+    ang = phantom.angles_deg(nang)
+    ofs = O.radon_struct(ang, N, N)
+    rng = np.random.default_rng(0)
+
+    def solver(Nz):
+        f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
+        return O.Solver(3, N, Nz, C, N, ofs, f, W["alpha"], W["mu"], 100.0, O.KL, O.TGV, O.FROB)
+
+    probe = solver(2)
+    t0 = time.perf_counter()
+    probe.run(1)
+    per_slice = (time.perf_counter() - t0) / 2
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    Nz = int(max(2, min(W["Nz"], budget / max(per_slice, 1e-6))))
+    s = solver(Nz)
+    s.run(args.warmup)
+    t0 = time.perf_counter()
+    s.run(args.steps)
+    dt = time.perf_counter() - t0
+    V = N * N * Nz * C
+    value = V * args.steps / dt
+    sample = (f"each step one iteration over 256x256x{Nz} slices x 4 channels, 71 angles (oracle/tgv_oracle.c, "
+              f"bit-exact with the reference kernels, OpenMP {os.cpu_count()} threads)")
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "sample_slices": Nz},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": os.cpu_count(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    from graptor_gb300 import radon_tgv_primal_dual_3d as r3
+    from graptor_gb300.solver import Problem
+    torch.cuda.set_device(local)
+    N, Nz, C, nang = W["N"], W["Nz"], W["C"], W["nang"]
+    sino, ang = make_problem_data(seed=rank)
+    S = C * Nz
+    V = N * N * S
+    Sb = N * nang * S
+    f = np.concatenate([np.transpose(s, (1, 0, 2)) for s in sino])  # [S, nang, nd]
+    stream = torch.cuda.Stream()
+    prob = Problem(3, N, Nz, C, N, ang, W["alpha"], W["mu"], "KL", "TGV", "FROB", 1.0, None, local,
+                   stream.cuda_stream)
+    prob.set_data(f)
+    prob.run(args.warmup).synchronize()
+
+    # ---- device-timed region: K iterations, inputs resident in HBM
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        prob.run(args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    clocks = clk.summary()
+    value = world * V * args.steps / (ms / 1e3)
+
+    # ---- per-kernel durations (CUDA events on the launching stream) for the roofline
+    kms = prob.time_kernels(reps=5)
+    alg = algorithmic_bytes(V, Sb)
+    top = max(kms, key=kms.get)
+    hbm, peak_kind = peaks()
+    achieved = alg[top] / (kms[top] / 1e3) / 1e9
+    traffic = ncu_traffic(top)
+    it_ms = ms / args.steps
+    solver_gbs = alg["iteration"] / (it_ms / 1e3) / 1e9
+    launches = prob.launches_per_iteration * args.steps
+    ne = prob.scalars["normest"]
+    prob.close()
+
+    # ---- end to end through the reference-facing entry point, host buffers
+    r3.progress = False
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    u, s_out = r3.Reconstructionapproach3d(sino, ang, W["alpha"], np.array(W["mu"]), args.steps, local, [0, 0.1], 1,
+                                           "KL", "Frobenius 3D Reconstruction", "TGV", [0.0, 1.0, [0]])
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    h2d = 4 * Sb
+    d2h = 4 * V + 4 * Sb
+    e2e = {"value": world * V * args.steps / e2e_s, "unit": METRIC,
+           "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+           "seconds": e2e_s, "includes": "problem setup, H2D of the sinograms, FP64 operator-norm estimate, "
+                                         "K iterations, D2H of Solution and Sinogram (one call)"}
+    if rank != 0:
+        return None
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": it_ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantoms, Poisson noise)",
+           "config": {"workload": WORKLOAD_NAME, "voxel_channels": V, "sinogram_bins": Sb, "dim": 3, "N": N,
+                      "Nz": Nz, "C": C, "nang": nang, "coupling": "FROB", "discrepancy": "KL",
+                      "regularisation": "TGV", "stated_iterations": W["stated_iterations"],
+                      "time_for_stated_iterations_s": it_ms * W["stated_iterations"] / 1e3,
+                      "l2": "inputs larger than L2 (solver state 1.1 GB per replica)",
+                      "parallelism": f"replicas x{world}", "normest": ne},
+           "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
+                        "algorithmic_bytes_per_launch": alg[top], "ms_per_launch": kms[top]},
+           "kernels_ms": kms,
+           "solver_roofline": {"achieved": solver_gbs, "peak": hbm, "unit": "GB/s", "frac": solver_gbs / hbm,
+                               "algorithmic_bytes_per_iteration": alg["iteration"]},
+           "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline()
+    return out
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        from oracle import oracle as O
+        O.build()  # the CPU-baseline leg needs the oracle library (built before any GPU work)
+        out = run_ours(args, rank, world, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

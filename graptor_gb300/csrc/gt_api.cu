@@ -1,0 +1,472 @@
+// C ABI of the GB300 primal-dual TGV/TV reconstruction (declared in
+// include/graptor_gb300.h): problem handles, host<->device layout changes,
+// step-size setup and the graph-captured iteration loop.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "graptor_gb300.h"
+#include "gt_common.cuh"
+
+namespace gt {
+cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st);
+cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st);
+cudaError_t launch_primal(const IterParams &P, int tgv, cudaStream_t st);
+cudaError_t launch_radon(const float *img, float *sino, const float4 *ofs, int N, int nd, int nang, int S,
+                         cudaStream_t st);
+cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, int N, int nd, int nang, int S,
+                            cudaStream_t st);
+cudaError_t launch_transpose(const float *in, float *out, int rows, int cols, cudaStream_t st);
+cudaError_t launch_feasible(float *f, const float *r1, int nbin1, int S, cudaStream_t st);
+cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, double *d_img, double *d_sino,
+                      double *d_part, double *out, cudaStream_t st);
+cudaError_t fill_f64(double *x, size_t n, double v, cudaStream_t st);
+cudaError_t fill_f32(float *x, size_t n, float v, cudaStream_t st);
+}  // namespace gt
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_err(cudaError_t e, const char *what, int line) {
+  cudaGetLastError();  // clear a sticky-free error so the next call starts clean
+  const int code = (e == cudaErrorMemoryAllocation) ? GT_ERR_OOM : GT_ERR_CUDA;
+  return set_err(code, "%s failed (line %d): %s", what, line, cudaGetErrorString(e));
+}
+
+#define CK(call)                                                         \
+  do {                                                                   \
+    cudaError_t e_ = (call);                                             \
+    if (e_ != cudaSuccess) return cuda_err(e_, #call, __LINE__);         \
+  } while (0)
+
+// Angle table of radon_struct (radon_tgv_primal_dual_3d.py:947-979): per angle
+// (X, Y, offset, Xinv) = (cos, sin, centring offset, 1/cos) in double, with
+// near-vertical rays (|1/cos| > 10 nd) made exactly vertical.  Detector width 1,
+// shift 0 (the reference's defaults, which its callers never change).
+void angle_table(const double *angles, int N, int nd, int nang, std::vector<double> &t64) {
+  t64.assign((size_t)nang * 4, 0.0);
+  const double mid_dom = (N - 1) / 2.0, mid_det = (nd - 1.0) / 2.0;
+  for (int j = 0; j < nang; ++j) {
+    double X = std::cos(angles[j]), Y = std::sin(angles[j]), Xinv = 1.0 / X;
+    if (std::fabs(Xinv) > 10.0 * nd) {
+      X = 0.0;
+      Y = std::nearbyint(std::sin(angles[j]));  // NumPy round(): half to even
+      Xinv = 0.0;
+    }
+    t64[4 * j + 0] = X;
+    t64[4 * j + 1] = Y;
+    t64[4 * j + 2] = mid_det - X * mid_dom - Y * mid_dom;
+    t64[4 * j + 3] = Xinv;
+  }
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct gt_problem {
+  gt::Dims d{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int disc = GT_KL, reg = GT_TGV, cpl = GT_FROB;
+  int K = 3, KW = 6;
+  float stepsize = 1.f;
+  double alpha0 = 4, alpha1 = 1, ne_in = 0, ne = 0, sigma = 0, tau = 0;
+  std::vector<double> mu, ofs64h;
+  void *block = nullptr;
+  float4 *ofs = nullptr;
+  dvec4 *ofs64 = nullptr;
+  float *mu_eff = nullptr;
+  float *u = nullptr, *ubar = nullptr, *p = nullptr, *pbar = nullptr, *v = nullptr, *w = nullptr;
+  float *lam = nullptr, *f = nullptr, *ku = nullptr, *stage = nullptr;
+  gt::IterParams P{};
+  cudaGraphExec_t g_one = nullptr, g_chunk = nullptr;
+  int chunk = 16;
+  long long iters = 0;
+  bool has_data = false;
+};
+
+namespace {
+
+int enqueue_iteration(gt_problem *p) {
+  CK(gt::launch_dual(p->P, p->reg == GT_TGV, p->cpl, p->stream));
+  CK(gt::launch_fwd(p->P, p->disc, p->stream));
+  CK(gt::launch_primal(p->P, p->reg == GT_TGV, p->stream));
+  return GT_OK;
+}
+
+int capture(gt_problem *p, int n, cudaGraphExec_t *out) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = GT_OK;
+  for (int k = 0; k < n && rc == GT_OK; ++k) rc = enqueue_iteration(p);
+  cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+  if (rc != GT_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_err(e, "cudaStreamEndCapture", __LINE__);
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_err(e, "cudaGraphInstantiate", __LINE__);
+  return GT_OK;
+}
+
+// device field -> (pointer, components, per-component X extent)
+int field_info(gt_problem *p, int field, float **ptr, int *comps, size_t *X) {
+  const size_t img = (size_t)p->d.N * p->d.N, sino = (size_t)p->d.nd * p->d.nang;
+  switch (field) {
+    case GT_U: *ptr = p->u; *comps = 1; *X = img; break;
+    case GT_UBAR: *ptr = p->ubar; *comps = 1; *X = img; break;
+    case GT_P: *ptr = p->p; *comps = p->K; *X = img; break;
+    case GT_PBAR: *ptr = p->pbar; *comps = p->K; *X = img; break;
+    case GT_V: *ptr = p->v; *comps = p->K; *X = img; break;
+    case GT_W: *ptr = p->w; *comps = p->KW; *X = img; break;
+    case GT_LAMBDA: *ptr = p->lam; *comps = 1; *X = sino; break;
+    case GT_KU: *ptr = p->ku; *comps = 1; *X = sino; break;
+    case GT_DATA: *ptr = p->f; *comps = 1; *X = sino; break;
+    default: return set_err(GT_ERR_ARG, "unknown state field %d", field);
+  }
+  if (!*ptr) return set_err(GT_ERR_ARG, "state field %d does not exist for this regularisation", field);
+  return GT_OK;
+}
+
+void set_scalars(gt_problem *p) {
+  // tgv_radon :1178-1189 (3-D) / :753-762 (2-D)
+  const double Lsqr = p->d.dim == 3 ? 17.0 : 0.5 * (18.0 + std::sqrt(33.0));
+  p->sigma = 1.0 / std::sqrt(Lsqr);
+  p->tau = p->sigma;
+  const double ne2 = p->ne * p->ne;
+  const double a0 = p->alpha0 / ne2, a1 = p->alpha1 / ne2;
+  p->P.sigma = (float)p->sigma;
+  p->P.tau = (float)p->tau;
+  p->P.sigma_data = (float)(p->sigma / p->ne);
+  p->P.norming = (float)(1.0 / p->ne);
+  p->P.ainv0 = (float)(1.0 / a0);
+  p->P.ainv1 = (float)(1.0 / a1);
+  p->P.stepsize = p->stepsize;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gt_last_error(void) { return g_err.c_str(); }
+const char *gt_version(void) { return "graptor_gb300 0.1 (sm_103a)"; }
+
+int gt_launches_per_iteration(const gt_problem *p) {
+  if (!p) return 0;
+  return 2 + (p->d.C > 8 ? (p->d.C + 7) / 8 : 1);
+}
+
+int gt_problem_create(const gt_desc *desc, gt_problem **out) {
+  if (!desc || !out) return set_err(GT_ERR_ARG, "null argument");
+  *out = nullptr;
+  const gt_desc &D = *desc;
+  if (D.dim != 2 && D.dim != 3) return set_err(GT_ERR_ARG, "dim must be 2 or 3 (got %d)", D.dim);
+  if (D.N < 1 || D.Nz < 1 || D.C < 1 || D.nd < 1 || D.nang < 1)
+    return set_err(GT_ERR_ARG, "sizes must be positive (N=%d Nz=%d C=%d nd=%d nang=%d)", D.N, D.Nz, D.C, D.nd, D.nang);
+  if (D.coupling != GT_UNCORR && D.C > 8)
+    return set_err(GT_ERR_ARG, "coupled regularisation supports at most 8 channels (got %d)", D.C);
+  if (D.discrepancy != GT_KL && D.discrepancy != GT_L2) return set_err(GT_ERR_ARG, "bad discrepancy");
+  if (D.regularisation != GT_TV && D.regularisation != GT_TGV) return set_err(GT_ERR_ARG, "bad regularisation");
+  if (D.coupling < GT_UNCORR || D.coupling > GT_NUCL) return set_err(GT_ERR_ARG, "bad coupling");
+  if (!D.angles || !D.mu) return set_err(GT_ERR_ARG, "angles and mu are required");
+  if (!(D.stepsize > 0.f)) return set_err(GT_ERR_ARG, "stepsize must be positive");
+  if (D.regularisation == GT_TGV && !(D.alpha0 > 0 && D.alpha1 > 0)) return set_err(GT_ERR_ARG, "alpha must be positive");
+  if (D.regularisation == GT_TV && !(D.alpha1 > 0)) return set_err(GT_ERR_ARG, "alpha1 must be positive");
+  const long long S = (long long)D.Nz * D.C;
+  const long long vol = (long long)D.N * D.N * S, nbin = (long long)D.nd * D.nang * S;
+  if ((long long)D.N * D.N > (1LL << 30) || S > (1LL << 20) || (long long)D.nd * D.nang > (1LL << 30))
+    return set_err(GT_ERR_ARG, "problem too large for 32-bit pixel / bin indices");
+
+  gt_problem *p = new (std::nothrow) gt_problem();
+  if (!p) return set_err(GT_ERR_OOM, "host allocation failed");
+  p->device = D.device;
+  p->d.dim = D.dim; p->d.N = D.N; p->d.Nz = D.Nz; p->d.C = D.C; p->d.S = (int)S;
+  p->d.nd = D.nd; p->d.nang = D.nang; p->d.vol = (size_t)vol; p->d.nbin = (size_t)nbin;
+  p->disc = D.discrepancy; p->reg = D.regularisation; p->cpl = D.coupling;
+  p->K = D.dim; p->KW = D.dim == 3 ? 6 : 3;
+  p->stepsize = D.stepsize;
+  p->alpha0 = D.alpha0; p->alpha1 = D.alpha1; p->ne_in = D.normest;
+  p->mu.assign(D.mu, D.mu + D.C);
+  angle_table(D.angles, D.N, D.nd, D.nang, p->ofs64h);
+
+  auto fail = [&](int rc) { gt_problem_destroy(p); return rc; };
+  if (cudaSetDevice(D.device) != cudaSuccess) return fail(cuda_err(cudaGetLastError(), "cudaSetDevice", __LINE__));
+  if (D.stream) {
+    p->stream = (cudaStream_t)D.stream;
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(cuda_err(e, "cudaStreamCreate", __LINE__));
+    p->own_stream = true;
+  }
+  const bool tgv = D.regularisation == GT_TGV;
+  const size_t fv = sizeof(float) * (size_t)vol, fb = sizeof(float) * (size_t)nbin;
+  size_t off[16], total = 0;
+  size_t sizes[] = {
+      align256(sizeof(float4) * D.nang), align256(sizeof(dvec4) * D.nang), align256(sizeof(float) * D.C),
+      align256(fv), align256(fv),                                   // u, ubar
+      tgv ? align256(fv * p->K) : 0, tgv ? align256(fv * p->K) : 0, // p, pbar
+      align256(fv * p->K),                                          // v
+      tgv ? align256(fv * p->KW) : 0,                               // w
+      align256(fb), align256(fb), align256(fb),                     // lam, f, ku
+      align256(std::max(fv, fb))};                                  // stage
+  const int nsz = (int)(sizeof(sizes) / sizeof(sizes[0]));
+  for (int k = 0; k < nsz; ++k) { off[k] = total; total += sizes[k]; }
+  cudaError_t e = cudaMalloc(&p->block, total);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    gt_problem_destroy(p);
+    return set_err(GT_ERR_OOM, "device allocation of %.3f GB failed: %s", total / 1e9, cudaGetErrorString(e));
+  }
+  char *b = (char *)p->block;
+  p->ofs = (float4 *)(b + off[0]);
+  p->ofs64 = (dvec4 *)(b + off[1]);
+  p->mu_eff = (float *)(b + off[2]);
+  p->u = (float *)(b + off[3]);
+  p->ubar = (float *)(b + off[4]);
+  p->p = tgv ? (float *)(b + off[5]) : nullptr;
+  p->pbar = tgv ? (float *)(b + off[6]) : nullptr;
+  p->v = (float *)(b + off[7]);
+  p->w = tgv ? (float *)(b + off[8]) : nullptr;
+  p->lam = (float *)(b + off[9]);
+  p->f = (float *)(b + off[10]);
+  p->ku = (float *)(b + off[11]);
+  p->stage = (float *)(b + off[12]);
+
+  std::vector<float> t32((size_t)D.nang * 4);
+  for (size_t k = 0; k < t32.size(); ++k) t32[k] = (float)p->ofs64h[k];
+  // zero the whole block first, then upload the angle tables into it
+  if ((e = cudaMemsetAsync(p->block, 0, total, p->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(p->ofs, t32.data(), sizeof(float) * t32.size(), cudaMemcpyHostToDevice, p->stream)) !=
+          cudaSuccess ||
+      (e = cudaMemcpyAsync(p->ofs64, p->ofs64h.data(), sizeof(double) * p->ofs64h.size(), cudaMemcpyHostToDevice,
+                           p->stream)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(p->stream)) != cudaSuccess)
+    return fail(cuda_err(e, "problem setup", __LINE__));
+
+  gt::IterParams &P = p->P;
+  P.d = p->d;
+  P.ofs = p->ofs; P.mu = p->mu_eff;
+  P.u = p->u; P.ubar = p->ubar; P.p = p->p; P.pbar = p->pbar; P.v = p->v; P.w = p->w;
+  P.lam = p->lam; P.f = p->f; P.ku = p->ku;
+  *out = p;
+  return GT_OK;
+}
+
+void gt_problem_destroy(gt_problem *p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  if (p->g_one) cudaGraphExecDestroy(p->g_one);
+  if (p->g_chunk) cudaGraphExecDestroy(p->g_chunk);
+  if (p->block) cudaFree(p->block);
+  if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+}
+
+int gt_set_data(gt_problem *p, const float *f_host, int make_feasible) {
+  if (!p || !f_host) return set_err(GT_ERR_ARG, "null argument");
+  CK(cudaSetDevice(p->device));
+  const gt::Dims &d = p->d;
+  const int nb1 = d.nd * d.nang;
+  CK(cudaMemcpyAsync(p->stage, f_host, sizeof(float) * d.nbin, cudaMemcpyHostToDevice, p->stream));
+  CK(gt::launch_transpose(p->stage, p->f, d.S, nb1, p->stream));
+  if (make_feasible) {
+    // Make_function_feasible (3-D :860-870): bins the all-ones slice does not reach
+    // (R 1 <= 0) are zeroed in every slice.  ku is free scratch here.
+    float *ones = p->stage, *r1 = p->ku;
+    CK(gt::fill_f32(ones, (size_t)d.N * d.N, 1.f, p->stream));
+    CK(gt::launch_radon(ones, r1, p->ofs, d.N, d.nd, d.nang, 1, p->stream));
+    CK(gt::launch_feasible(p->f, r1, nb1, d.S, p->stream));
+  }
+  // operator norm (radon_normest, 3-D :1018-1030): injected, or FP64 power iteration
+  if (p->ne_in > 0) {
+    p->ne = p->ne_in;
+  } else {
+    const size_t n = (size_t)d.N * d.N;
+    double *scratch = nullptr;
+    const size_t bytes = sizeof(double) * (n + (size_t)nb1 + 256);
+    cudaError_t e = cudaMalloc(&scratch, bytes);
+    if (e != cudaSuccess) return cuda_err(e, "cudaMalloc (normest scratch)", __LINE__);
+    double ne = 0;
+    e = gt::fill_f64(scratch, n, 1.0, p->stream);
+    if (e == cudaSuccess)
+      e = gt::normest64(p->ofs64, d.N, d.nd, d.nang, 30, scratch, scratch + n, scratch + n + nb1, &ne, p->stream);
+    cudaFree(scratch);
+    if (e != cudaSuccess) return cuda_err(e, "normest64", __LINE__);
+    if (!(ne > 0) || !std::isfinite(ne)) return set_err(GT_ERR_CUDA, "operator norm estimate failed (%g)", ne);
+    p->ne = ne;
+  }
+  set_scalars(p);
+  // channel weights: KL mu, L2 mu/(sigma+mu) (3-D :1186-1189)
+  std::vector<float> me(d.C);
+  for (int c = 0; c < d.C; ++c)
+    me[c] = (float)(p->disc == GT_KL ? p->mu[c] : p->mu[c] / (p->sigma + p->mu[c]));
+  CK(cudaMemcpyAsync(p->mu_eff, me.data(), sizeof(float) * d.C, cudaMemcpyHostToDevice, p->stream));
+  // zero iterates (tgv_radon :1160-1176)
+  const size_t fv = sizeof(float) * d.vol;
+  CK(cudaMemsetAsync(p->u, 0, fv, p->stream));
+  CK(cudaMemsetAsync(p->ubar, 0, fv, p->stream));
+  if (p->p) CK(cudaMemsetAsync(p->p, 0, fv * p->K, p->stream));
+  if (p->pbar) CK(cudaMemsetAsync(p->pbar, 0, fv * p->K, p->stream));
+  CK(cudaMemsetAsync(p->v, 0, fv * p->K, p->stream));
+  if (p->w) CK(cudaMemsetAsync(p->w, 0, fv * p->KW, p->stream));
+  CK(cudaMemsetAsync(p->lam, 0, sizeof(float) * d.nbin, p->stream));
+  CK(cudaMemsetAsync(p->ku, 0, sizeof(float) * d.nbin, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  // the step scalars are baked into the captured graphs: recapture
+  if (p->g_one) { cudaGraphExecDestroy(p->g_one); p->g_one = nullptr; }
+  if (p->g_chunk) { cudaGraphExecDestroy(p->g_chunk); p->g_chunk = nullptr; }
+  p->iters = 0;
+  p->has_data = true;
+  return GT_OK;
+}
+
+int gt_run(gt_problem *p, int iters) {
+  if (!p) return set_err(GT_ERR_ARG, "null problem");
+  if (!p->has_data) return set_err(GT_ERR_STATE, "gt_run before gt_set_data");
+  if (iters < 0) return set_err(GT_ERR_ARG, "negative iteration count");
+  if (iters == 0) return GT_OK;
+  CK(cudaSetDevice(p->device));
+  int rc;
+  if (iters >= p->chunk && !p->g_chunk && (rc = capture(p, p->chunk, &p->g_chunk)) != GT_OK) return rc;
+  if (!p->g_one && (rc = capture(p, 1, &p->g_one)) != GT_OK) return rc;
+  int left = iters;
+  while (left >= p->chunk) { CK(cudaGraphLaunch(p->g_chunk, p->stream)); left -= p->chunk; }
+  while (left > 0) { CK(cudaGraphLaunch(p->g_one, p->stream)); --left; }
+  p->iters += iters;
+  return GT_OK;
+}
+
+int gt_synchronize(gt_problem *p) {
+  if (!p) return set_err(GT_ERR_ARG, "null problem");
+  CK(cudaSetDevice(p->device));
+  CK(cudaStreamSynchronize(p->stream));
+  return GT_OK;
+}
+
+int gt_get_state(gt_problem *p, int field, float *host) {
+  if (!p || !host) return set_err(GT_ERR_ARG, "null argument");
+  float *ptr; int comps; size_t X;
+  int rc = field_info(p, field, &ptr, &comps, &X);
+  if (rc) return rc;
+  CK(cudaSetDevice(p->device));
+  const size_t S = p->d.S;
+  for (int k = 0; k < comps; ++k) {
+    const size_t plane = (field == GT_LAMBDA || field == GT_KU || field == GT_DATA) ? p->d.nbin : p->d.vol;
+    CK(gt::launch_transpose(ptr + k * plane, p->stage, (int)X, (int)S, p->stream));
+    CK(cudaMemcpyAsync(host + k * X * S, p->stage, sizeof(float) * X * S, cudaMemcpyDeviceToHost, p->stream));
+  }
+  CK(cudaStreamSynchronize(p->stream));
+  return GT_OK;
+}
+
+int gt_set_state(gt_problem *p, int field, const float *host) {
+  if (!p || !host) return set_err(GT_ERR_ARG, "null argument");
+  float *ptr; int comps; size_t X;
+  int rc = field_info(p, field, &ptr, &comps, &X);
+  if (rc) return rc;
+  CK(cudaSetDevice(p->device));
+  const size_t S = p->d.S;
+  for (int k = 0; k < comps; ++k) {
+    const size_t plane = (field == GT_LAMBDA || field == GT_KU || field == GT_DATA) ? p->d.nbin : p->d.vol;
+    CK(cudaMemcpyAsync(p->stage, host + k * X * S, sizeof(float) * X * S, cudaMemcpyHostToDevice, p->stream));
+    CK(gt::launch_transpose(p->stage, ptr + k * plane, (int)S, (int)X, p->stream));
+  }
+  CK(cudaStreamSynchronize(p->stream));
+  return GT_OK;
+}
+
+int gt_get_scalars(gt_problem *p, double out[4]) {
+  if (!p || !out) return set_err(GT_ERR_ARG, "null argument");
+  out[0] = p->ne; out[1] = p->sigma; out[2] = p->tau; out[3] = (double)p->iters;
+  return GT_OK;
+}
+
+int gt_gap(gt_problem *p, double out[4]) {
+  (void)p; (void)out;
+  return set_err(GT_ERR_STATE, "gt_gap: not available in this build");
+}
+
+int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n) {
+  if (!p || !ms_out || reps < 1 || n < 3) return set_err(GT_ERR_ARG, "bad argument");
+  if (!p->has_data) return set_err(GT_ERR_STATE, "gt_time_kernels before gt_set_data");
+  CK(cudaSetDevice(p->device));
+  cudaEvent_t ev[4];
+  for (auto &e : ev) CK(cudaEventCreate(&e));
+  float acc[3] = {0, 0, 0};
+  int rc = GT_OK;
+  for (int r = 0; r < reps && rc == GT_OK; ++r) {
+    cudaError_t e;
+    if ((e = cudaEventRecord(ev[0], p->stream)) != cudaSuccess) { rc = cuda_err(e, "event", __LINE__); break; }
+    if ((e = gt::launch_dual(p->P, p->reg == GT_TGV, p->cpl, p->stream)) != cudaSuccess) { rc = cuda_err(e, "k_dual", __LINE__); break; }
+    cudaEventRecord(ev[1], p->stream);
+    if ((e = gt::launch_fwd(p->P, p->disc, p->stream)) != cudaSuccess) { rc = cuda_err(e, "k_fwd", __LINE__); break; }
+    cudaEventRecord(ev[2], p->stream);
+    if ((e = gt::launch_primal(p->P, p->reg == GT_TGV, p->stream)) != cudaSuccess) { rc = cuda_err(e, "k_primal", __LINE__); break; }
+    cudaEventRecord(ev[3], p->stream);
+    if ((e = cudaEventSynchronize(ev[3])) != cudaSuccess) { rc = cuda_err(e, "event sync", __LINE__); break; }
+    for (int k = 0; k < 3; ++k) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+      acc[k] += ms;
+    }
+    p->iters += 1;
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (rc) return rc;
+  for (int k = 0; k < 3; ++k) ms_out[k] = acc[k] / reps;
+  return GT_OK;
+}
+
+static int run_projector(bool forward, const float *in, float *out, const double *angles, int N, int nd, int nang,
+                         int S, void *stream) {
+  if (!in || !out || !angles) return set_err(GT_ERR_ARG, "null argument");
+  if (N < 1 || nd < 1 || nang < 1 || S < 1) return set_err(GT_ERR_ARG, "sizes must be positive");
+  std::vector<double> t64;
+  angle_table(angles, N, nd, nang, t64);
+  std::vector<float> t32(t64.size());
+  for (size_t k = 0; k < t64.size(); ++k) t32[k] = (float)t64[k];
+  cudaStream_t st = (cudaStream_t)stream;
+  float4 *ofs = nullptr;
+  CK(cudaMalloc(&ofs, sizeof(float4) * nang));
+  cudaError_t e = cudaMemcpyAsync(ofs, t32.data(), sizeof(float4) * nang, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = forward ? gt::launch_radon(in, out, ofs, N, nd, nang, S, st) : gt::launch_radon_ad(in, out, ofs, N, nd, nang, S, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(ofs);
+  if (e != cudaSuccess) return cuda_err(e, forward ? "radon" : "radon_ad", __LINE__);
+  return GT_OK;
+}
+
+int gt_radon(const float *img_dev, float *sino_dev, const double *angles, int N, int nd, int nang, int S,
+             void *stream) {
+  return run_projector(true, img_dev, sino_dev, angles, N, nd, nang, S, stream);
+}
+
+int gt_radon_ad(const float *sino_dev, float *img_dev, const double *angles, int N, int nd, int nang, int S,
+                void *stream) {
+  return run_projector(false, sino_dev, img_dev, angles, N, nd, nang, S, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,52 @@
+// Shared definitions of the GB300 TGV/TV primal-dual solver kernels.
+//
+// Device layout ("slice-fastest"): for every image-domain field the S = C*Nz
+// slice-channel values of one pixel are contiguous,
+//     image field   f[(y*N + x)*S + s]            s = c*Nz + z
+//     sinogram      g[(j*nd + i)*S + s]           j = angle, i = detector bin
+//     vector / tensor fields: one such plane per component, planes `vol` apart.
+// With s fastest, the per-pixel geometry of the projectors (detector coordinate,
+// interpolation weights, loop bounds) is the same for every lane of a warp, and
+// every global access of a warp is one contiguous run of slice values.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+// 4 doubles, 32-byte aligned (the FP64 angle table entry)
+struct __align__(32) dvec4 {
+  double x, y, z, w;
+};
+
+namespace gt {
+
+enum { KL = 0, L2 = 1 };
+enum { UNCORR = 0, FROB = 1, NUCL = 2 };
+
+struct Dims {
+  int dim;     // 2 or 3
+  int N, Nz, C, S;
+  int nd, nang;
+  size_t vol;  // N*N*S
+  size_t nbin; // nd*nang*S
+};
+
+// parameters of one iteration (the float32 kernel arguments of tgv_radon,
+// radon_tgv_primal_dual_3d.py:1178-1221)
+struct IterParams {
+  Dims d;
+  float sigma, tau;      // primal/dual steps 1/sqrt(Lsqr)
+  float sigma_data;      // sigma / normest (update_lambda argument)
+  float norming;         // 1 / normest     (update_u argument)
+  float ainv0, ainv1;    // 1 / (alpha / normest^2)
+  float stepsize;
+  int cbase;             // first channel handled by a k_dual launch (0 unless C > 8)
+  const float4 *ofs;     // [nang] (X, Y, offset, Xinv)
+  const float *mu;       // [C] mu (KL) or mu/(sigma+mu) (L2)
+  float *u, *ubar;       // [vol]
+  float *p, *pbar, *v;   // [K][vol]
+  float *w;              // [KW][vol]
+  float *lam, *f, *ku;   // [nbin]
+};
+
+}  // namespace gt

@@ -1,0 +1,153 @@
+"""Host-side problem handle over the C ABI.
+
+:class:`Problem` is one reconstruction problem resident on one GPU: it owns the
+device state of the reference's tgv_radon (U, U_, P, P_, V, W, Lamb, F;
+radon_tgv_primal_dual_3d.py:1160-1176) and runs graph-captured iterations.
+Host arrays use the reference solver's layouts (see include/graptor_gb300.h).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+DISCREPANCY = {"KL": L.GT_KL, "L2": L.GT_L2}
+REGULARISATION = {"TV": L.GT_TV, "TGV": L.GT_TGV}
+COUPLING = {"UNCORR": L.GT_UNCORR, "FROB": L.GT_FROB, "NUCL": L.GT_NUCL}
+
+# Reconstruction_coupled.py:971-995 method strings -> (dim, coupling)
+METHODS = {
+    "Uncorrelated 2D Reconstruction": (2, "UNCORR"), "Frobenius 2D Reconstruction": (2, "FROB"),
+    "Nuclear 2D Reconstruction": (2, "NUCL"), "Uncorrelated 3D Reconstruction": (3, "UNCORR"),
+    "Frobenius 3D Reconstruction": (3, "FROB"), "Nuclear 3D Reconstruction": (3, "NUCL"),
+}
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Problem:
+    """One TGV/TV primal-dual problem on the GPU.
+
+    Parameters mirror Reconstructionapproach2d/3d: ``angles`` in radians already
+    shifted by +pi/2, ``alpha = (alpha0, alpha1)``, ``mu`` per channel,
+    ``stepsize`` the slice step.  ``normest=None`` estimates the operator norm by
+    an FP64 power iteration on the device; a positive value is used as given.
+    """
+
+    def __init__(self, dim, N, Nz, C, nd, angles, alpha=(4.0, 1.0), mu=None, discrepancy="KL",
+                 regularisation="TGV", coupling="FROB", stepsize=1.0, normest=None, device=0, stream=None):
+        self._h = None
+        self.dim, self.N, self.Nz, self.C, self.nd = int(dim), int(N), int(Nz), int(C), int(nd)
+        self.angles = np.ascontiguousarray(angles, dtype=np.float64)
+        self.nang = int(self.angles.size)
+        self.S = self.Nz * self.C
+        self.K = self.dim
+        self.KW = 6 if self.dim == 3 else 3
+        alpha = np.atleast_1d(np.asarray(alpha, dtype=np.float64))
+        if alpha.size == 1:
+            alpha = np.array([alpha[0], alpha[0]])
+        self.mu = np.ascontiguousarray(np.ones(self.C) if mu is None else mu, dtype=np.float64)
+        if self.mu.size != self.C:
+            raise ValueError(f"mu has {self.mu.size} entries for {self.C} channels")
+        self.regularisation = regularisation.upper()
+        d = L.GtDesc()
+        d.dim, d.N, d.Nz, d.C, d.nd, d.nang = self.dim, self.N, self.Nz, self.C, self.nd, self.nang
+        d.angles = self.angles.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.stepsize = float(stepsize)
+        d.alpha0, d.alpha1 = float(alpha[0]), float(alpha[1])
+        d.mu = self.mu.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.discrepancy = DISCREPANCY[discrepancy.upper()]
+        d.regularisation = REGULARISATION[self.regularisation]
+        d.coupling = COUPLING[coupling.upper()]
+        d.normest = float(normest) if normest else 0.0
+        d.device = int(device)
+        d.stream = stream
+        h = ctypes.c_void_p()
+        L.check(L.lib().gt_problem_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+
+    # ------------------------------------------------------------------ lifecycle
+    def close(self):
+        if self._h is not None and self._h.value:
+            L.lib().gt_problem_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------------ data / iteration
+    def set_data(self, f, feasible: bool = True):
+        """Sinogram data ``f[S, nang, nd]`` (s = c*Nz + z); resets the iterates."""
+        f = np.ascontiguousarray(f, dtype=np.float32).reshape(self.S, self.nang, self.nd)
+        L.check(L.lib().gt_set_data(self._h, _ptr(f), int(bool(feasible))))
+        return self
+
+    def run(self, iters: int):
+        L.check(L.lib().gt_run(self._h, int(iters)))
+        return self
+
+    def synchronize(self):
+        L.check(L.lib().gt_synchronize(self._h))
+        return self
+
+    def _shape(self, field):
+        img, sino = (self.S, self.N, self.N), (self.S, self.nang, self.nd)
+        return {"u": img, "ubar": img, "p": (self.K,) + img, "pbar": (self.K,) + img, "v": (self.K,) + img,
+                "w": (self.KW,) + img, "lambda": sino, "ku": sino, "data": sino}[field]
+
+    def get(self, field: str) -> np.ndarray:
+        out = np.empty(self._shape(field), np.float32)
+        L.check(L.lib().gt_get_state(self._h, L.FIELDS[field], _ptr(out)))
+        return out
+
+    def set(self, field: str, value) -> None:
+        a = np.ascontiguousarray(value, dtype=np.float32).reshape(self._shape(field))
+        L.check(L.lib().gt_set_state(self._h, L.FIELDS[field], _ptr(a)))
+
+    @property
+    def scalars(self) -> dict:
+        out = (ctypes.c_double * 4)()
+        L.check(L.lib().gt_get_scalars(self._h, out))
+        return {"normest": out[0], "sigma": out[1], "tau": out[2], "iterations": int(out[3])}
+
+    def gap(self) -> dict:
+        out = (ctypes.c_double * 4)()
+        L.check(L.lib().gt_gap(self._h, out))
+        return {"primal": out[0], "dual": out[1], "gap": out[2], "relative": out[3]}
+
+    def time_kernels(self, reps: int = 5) -> dict:
+        """Mean CUDA-event duration (ms) of each kernel of one iteration."""
+        out = (ctypes.c_float * 3)()
+        L.check(L.lib().gt_time_kernels(self._h, int(reps), out, 3))
+        return {"k_dual": out[0], "k_fwd": out[1], "k_primal": out[2]}
+
+    @property
+    def launches_per_iteration(self) -> int:
+        return int(L.lib().gt_launches_per_iteration(self._h))
+
+
+def radon(img_dev, sino_dev, angles, N, nd, S, stream=None):
+    """Forward projection of device tensors (device layout [N*N][S] -> [nang*nd][S])."""
+    ang = np.ascontiguousarray(angles, dtype=np.float64)
+    L.check(L.lib().gt_radon(ctypes.c_void_p(img_dev), ctypes.c_void_p(sino_dev), _ptr(ang), int(N), int(nd),
+                             int(ang.size), int(S), stream))
+
+
+def radon_ad(sino_dev, img_dev, angles, N, nd, S, stream=None):
+    """Back projection of device tensors (device layout [nang*nd][S] -> [N*N][S])."""
+    ang = np.ascontiguousarray(angles, dtype=np.float64)
+    L.check(L.lib().gt_radon_ad(ctypes.c_void_p(sino_dev), ctypes.c_void_p(img_dev), _ptr(ang), int(N), int(nd),
+                                int(ang.size), int(S), stream))

@@ -1,0 +1,131 @@
+/*
+ * graptor_gb300.h -- C ABI of the GB300 primal-dual TGV/TV reconstruction library.
+ *
+ * The library replaces the device side of Graptor's solver: the OpenCL program
+ * and the enqueue loop of tgv_radon (radon_tgv_primal_dual_3d.py:96-848,
+ * :1135-1292; radon_tgv_primal_dual_2d.py:95-463, :710-851).  Python (or any
+ * FFI) keeps the reference's entry points Reconstructionapproach2d/3d and calls
+ * the functions below; graptor_gb300/radon_tgv_primal_dual_{2d,3d}.py are those
+ * adapters.
+ *
+ * Conventions
+ *  - Every function returns an int status: GT_OK or one of GT_ERR_*; no C++
+ *    exception crosses this boundary.  gt_last_error() gives the message of the
+ *    calling thread's last failure.
+ *  - Host arrays are caller-owned and copied; device memory is library-owned.
+ *  - A problem handle is bound to one CUDA device and one stream and is not
+ *    thread-safe; distinct handles may be used from distinct threads.
+ *  - Array layouts on the host side are the reference solver's, per channel c and
+ *    slice z with s = c*Nz + z (the reference's Nz*Number_Channels axis):
+ *        image  float32[S][N][N]     index (s*N + y)*N + x
+ *        sino   float32[S][nang][nd] index (s*nang + j)*nd + i
+ *    vector fields carry a leading component axis ([K][S][N][N]).
+ */
+#ifndef GRAPTOR_GB300_H
+#define GRAPTOR_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define GT_API __attribute__((visibility("default")))
+#else
+#define GT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (Reconstruction_coupled.py:509-536 maps OOM to a smaller chunk) */
+enum {
+  GT_OK = 0,
+  GT_ERR_OOM = 1,       /* device allocation failed  (reference: pyopencl.MemoryError) */
+  GT_ERR_ARG = 2,       /* invalid argument / unsupported configuration */
+  GT_ERR_TIMEOUT = 3,   /* a bounded device wait ran out */
+  GT_ERR_CUDA = 4,      /* any other CUDA failure      (reference: pyopencl.Error) */
+  GT_ERR_STATE = 5      /* call out of order (e.g. run before data) */
+};
+
+enum { GT_KL = 0, GT_L2 = 1 };               /* discrepancy,   radon_tgv_primal_dual_3d.py:1053-1068 */
+enum { GT_TV = 0, GT_TGV = 1 };              /* regularisation, :1040-1051 */
+enum { GT_UNCORR = 0, GT_FROB = 1, GT_NUCL = 2 }; /* coupling, :1079-1130 */
+
+/* state fields for gt_get_state / gt_set_state (the reference's U, U_, P, P_, V, W, Lamb) */
+enum { GT_U = 0, GT_UBAR = 1, GT_P = 2, GT_PBAR = 3, GT_V = 4, GT_W = 5, GT_LAMBDA = 6, GT_KU = 7, GT_DATA = 8 };
+
+/* Problem description.  Mirrors the argument surface of Reconstructionapproach2d/3d
+ * (radon_tgv_primal_dual_2d.py:69, radon_tgv_primal_dual_3d.py:69). */
+typedef struct gt_desc {
+  int dim;              /* 2: slice-wise 2-D (Nz independent slices), 3: volumetric */
+  int N;                /* image side; the reference always uses N = nd (3-D :1316) */
+  int Nz;               /* slices per channel */
+  int C;                /* channels */
+  int nd;               /* detector bins */
+  int nang;             /* projection angles */
+  const double *angles; /* radians, caller-shifted by +pi/2 as Reconstruction_coupled.py:233/:448 */
+  float stepsize;       /* slice step (3-D z-derivative divisor), Stepsize argument */
+  double alpha0;        /* second-order TGV weight, Parameter[0] */
+  double alpha1;        /* first-order weight,      Parameter[1] */
+  const double *mu;     /* [C] channel weights */
+  int discrepancy;      /* GT_KL / GT_L2 */
+  int regularisation;   /* GT_TV / GT_TGV */
+  int coupling;         /* GT_UNCORR / GT_FROB / GT_NUCL */
+  double normest;       /* > 0: use this operator-norm estimate; <= 0: FP64 power iteration on device */
+  int device;           /* CUDA device ordinal */
+  void *stream;         /* cudaStream_t to run on, or NULL for a library-owned stream */
+} gt_desc;
+
+typedef struct gt_problem gt_problem;
+
+/* Allocate device state for one problem (replaces tgv_radon's buffer setup,
+ * radon_tgv_primal_dual_3d.py:1147-1176, and radon_struct :947-979). */
+GT_API int gt_problem_create(const gt_desc *desc, gt_problem **out);
+GT_API void gt_problem_destroy(gt_problem *p);
+
+/* Upload the sinogram data f (host, [S][nang][nd]) and reset the iterates to zero.
+ * make_feasible != 0 applies Make_function_feasible (3-D :860-870).  This is also
+ * where the operator norm is estimated when desc.normest <= 0 (3-D :1018-1030). */
+GT_API int gt_set_data(gt_problem *p, const float *f_host, int make_feasible);
+
+/* Run iters primal-dual iterations (the loop body of 3-D :1194-1221), graph-captured,
+ * asynchronous on the problem's stream. */
+GT_API int gt_run(gt_problem *p, int iters);
+GT_API int gt_synchronize(gt_problem *p);
+
+/* Copy one state field to / from host memory in the layout described above.
+ * GT_U after gt_run is the reference's returned Solution, GT_KU its Sinogram. */
+GT_API int gt_get_state(gt_problem *p, int field, float *host);
+GT_API int gt_set_state(gt_problem *p, int field, const float *host);
+
+/* Scalars the run uses: [0] normest, [1] sigma, [2] tau, [3] iterations run. */
+GT_API int gt_get_scalars(gt_problem *p, double out[4]);
+
+/* FP64 primal-dual gap of the current iterate (the reference has none; draft
+ * at 3-D :882-927).  out: [0] primal energy, [1] dual energy, [2] gap P-D,
+ * [3] relative gap (P-D)/|P|. */
+GT_API int gt_gap(gt_problem *p, double out[4]);
+
+/* Standalone projectors on device memory in the library's device layout
+ * (image [N*N][S], sinogram [nang*nd][S]); for tests and data generation.
+ * Kernels `radon` (3-D :773-816) and `radon_ad` (3-D :818-844). */
+GT_API int gt_radon(const float *img_dev, float *sino_dev, const double *angles, int N, int nd, int nang, int S,
+             void *stream);
+GT_API int gt_radon_ad(const float *sino_dev, float *img_dev, const double *angles, int N, int nd, int nang, int S,
+                void *stream);
+
+/* Run reps iterations kernel by kernel (not graph-captured), timing each kernel
+ * with CUDA events on the problem stream; ms_out[0..2] receive the mean duration
+ * of k_dual, k_fwd and k_primal (n >= 3).  The iterations are real: the state
+ * advances by reps iterations. */
+GT_API int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n);
+
+/* Number of kernel launches one iteration issues (for launch accounting). */
+GT_API int gt_launches_per_iteration(const gt_problem *p);
+
+GT_API const char *gt_last_error(void);
+GT_API const char *gt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRAPTOR_GB300_H */
