@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 W = dict(N=256, Nz=60, C=4, nang=71, alpha=(4.0, 1.0), mu=[0.2, 5e-4, 4e-3, 5e-4], peaks=[1e4, 20.0, 20.0, 20.0],
          stated_iterations=2500)
 METRIC = "voxel-iter/s"
-WORKLOAD_NAME = "3D FROB3D TGV-KL 256x256x60, 4 channels, 256 bins x 71 angles"
+WORKLOAD_NAME = "3D FROB3D TGV-KL {N}x{N}x{Nz}, 4 channels, {N} bins x 71 angles"
 
 
 def peaks():
@@ -221,7 +221,7 @@ def run_reference(args, rank, world):
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME, "sample_slices": Nz},
+            "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"]), "sample_slices": Nz},
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": os.cpu_count(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -259,6 +259,11 @@ def run_ours(args, rank, world, local):
     ms = max_over_ranks(ev0.elapsed_time(ev1), world)
     clocks = clk.summary()
     value = world * V * args.steps / (ms / 1e3)
+    if args.quick:
+        prob.close()
+        return {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"]), "Nz": Nz, "quick": True}, "clocks": clocks}
 
     # ---- per-kernel durations (CUDA events on the launching stream) for the roofline
     kms = prob.time_kernels(reps=5)
@@ -292,7 +297,7 @@ def run_ours(args, rank, world, local):
     out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": it_ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantoms, Poisson noise)",
-           "config": {"workload": WORKLOAD_NAME, "voxel_channels": V, "sinogram_bins": Sb, "dim": 3, "N": N,
+           "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"]), "voxel_channels": V, "sinogram_bins": Sb, "dim": 3, "N": N,
                       "Nz": Nz, "C": C, "nang": nang, "coupling": "FROB", "discrepancy": "KL",
                       "regularisation": "TGV", "stated_iterations": W["stated_iterations"],
                       "time_for_stated_iterations_s": it_ms * W["stated_iterations"] / 1e3,
@@ -330,7 +335,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nz", type=int, default=None,
+                    help="slices per channel (default 60); smaller cases for profiler captures")
+    ap.add_argument("--n", type=int, default=None, help="image side (default 256); profiler captures")
+    ap.add_argument("--quick", action="store_true",
+                    help="only the device-timed region (no e2e, kernel timing or CPU baseline): profiler runs")
     args = ap.parse_args()
+    if args.nz:
+        W["Nz"] = int(args.nz)
+    if args.n:
+        W["N"] = int(args.n)
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         out = run_reference(args, rank, world)

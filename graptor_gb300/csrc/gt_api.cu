@@ -85,6 +85,8 @@ struct gt_problem {
   gt::Dims d{};
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;            // second stream: k_fwd runs beside k_dual
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool own_stream = false;
   int disc = GT_KL, reg = GT_TGV, cpl = GT_FROB;
   int K = 3, KW = 6;
@@ -106,9 +108,16 @@ struct gt_problem {
 
 namespace {
 
+// One iteration.  k_dual (memory-bound) and k_fwd (issue-bound) touch disjoint
+// outputs and only read what the previous k_primal wrote, so they run on two
+// streams and overlap; k_primal waits for both (a fork/join in the graph).
 int enqueue_iteration(gt_problem *p) {
+  CK(cudaEventRecord(p->ev_fork, p->stream));
+  CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
+  CK(gt::launch_fwd(p->P, p->disc, p->side));
   CK(gt::launch_dual(p->P, p->reg == GT_TGV, p->cpl, p->stream));
-  CK(gt::launch_fwd(p->P, p->disc, p->stream));
+  CK(cudaEventRecord(p->ev_join, p->side));
+  CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
   CK(gt::launch_primal(p->P, p->reg == GT_TGV, p->stream));
   return GT_OK;
 }
@@ -219,6 +228,12 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
     if (e != cudaSuccess) return fail(cuda_err(e, "cudaStreamCreate", __LINE__));
     p->own_stream = true;
   }
+  {
+    cudaError_t e1 = cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking);
+    if (e1 == cudaSuccess) e1 = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
+    if (e1 == cudaSuccess) e1 = cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming);
+    if (e1 != cudaSuccess) return fail(cuda_err(e1, "stream/event setup", __LINE__));
+  }
   const bool tgv = D.regularisation == GT_TGV;
   const size_t fv = sizeof(float) * (size_t)vol, fb = sizeof(float) * (size_t)nbin;
   size_t off[16], total = 0;
@@ -280,6 +295,9 @@ void gt_problem_destroy(gt_problem *p) {
   if (p->g_one) cudaGraphExecDestroy(p->g_one);
   if (p->g_chunk) cudaGraphExecDestroy(p->g_chunk);
   if (p->block) cudaFree(p->block);
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  if (p->ev_join) cudaEventDestroy(p->ev_join);
+  if (p->side) cudaStreamDestroy(p->side);
   if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
   delete p;
 }

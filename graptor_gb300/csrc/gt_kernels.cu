@@ -24,33 +24,45 @@ namespace gt {
 // ball projections
 // ===========================================================================
 
+// The nuclear-norm projections evaluate eigenvectors by formulas that cancel
+// catastrophically when the off-diagonal entry is small, so their results depend
+// on rounding: they are written with explicitly rounded operations (no fused
+// multiply-add), in the reference's order, and with hypot / atan / cos / cube
+// evaluated in double and rounded once (as the host C library's float versions
+// are, to within their last bit).
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float hyp(float a, float b) { return (float)sqrt((double)a * a + (double)b * b); }
+
 // nuclear 2-D (update_NormV_Nucl, radon_tgv_primal_dual_2d.py:124-204): spectral
-// projection of the C x 2 matrix A of one pixel via the 2x2 matrix A^T A.
+// projection of the C x 2 matrix A of one pixel via the 2x2 matrix A^T A = [a b; b c].
 __device__ __forceinline__ void nucl2d_matrix(float a, float b, float c, float ainv, float M[3]) {
   const float eps = 0.00001f;
   float s1, s2, S1, S2;
-  const float o = fminf(a, c);
-  if ((b * b) / (o * o) > eps && o * o > 0.f) {
-    const float dd = a + c, e = a - c;
-    float f = 4.f * b * b + e * e;
+  const float o = c < a ? c : a;
+  if (fm(b, b) / fm(o, o) > eps && fm(o, o) > 0.f) {
+    const float dd = fa(a, c), e = fs(a, c);
+    float f = fa(fm(fm(4.f, b), b), fm(e, e));
     f = f < 0.f ? 0.f : sqrtf(f);
-    s2 = (dd - f > 0.f) ? sqrtf((dd - f) * 0.5f) : 0.f;
-    s1 = (dd + f > 0.f) ? sqrtf((dd + f) * 0.5f) : 0.f;
-    const float g = (e + f) * 0.5f, h = (e - f) * 0.5f;
-    float q0 = g * a + b * b, q1 = g * b + c * b, q2 = h * a + b * b, q3 = h * b + b * c;
-    const float n1 = hypotf(q0, q1), n2 = hypotf(q2, q3);
+    s2 = (fs(dd, f) > 0.f) ? sqrtf(fm(fs(dd, f), 0.5f)) : 0.f;
+    s1 = (fa(dd, f) > 0.f) ? sqrtf(fm(fa(dd, f), 0.5f)) : 0.f;
+    const float g = fm(fa(e, f), 0.5f), h = fm(fs(e, f), 0.5f);
+    float q0 = fa(fm(g, a), fm(b, b)), q1 = fa(fm(g, b), fm(c, b));
+    float q2 = fa(fm(h, a), fm(b, b)), q3 = fa(fm(h, b), fm(b, c));
+    const float n1 = hyp(q0, q1), n2 = hyp(q2, q3);
     if (n1 > 0.f) { q0 = q0 / n1; q1 = q1 / n1; }
     if (n2 > 0.f) { q2 = q2 / n2; q3 = q3 / n2; }
-    S1 = (s1 * ainv > 1.f) ? 1.f / (s1 * ainv) : 1.f;
-    S2 = (s2 * ainv > 1.f) ? 1.f / (s2 * ainv) : 1.f;
-    M[0] = q0 * q0 * S1 + q2 * q2 * S2;
-    M[2] = q1 * q1 * S1 + q3 * q3 * S2;
-    M[1] = S1 * q0 * q1 + S2 * q2 * q3;
+    S1 = (fm(s1, ainv) > 1.f) ? 1.f / fm(s1, ainv) : 1.f;
+    S2 = (fm(s2, ainv) > 1.f) ? 1.f / fm(s2, ainv) : 1.f;
+    M[0] = fa(fm(fm(q0, q0), S1), fm(fm(q2, q2), S2));
+    M[2] = fa(fm(fm(q1, q1), S1), fm(fm(q3, q3), S2));
+    M[1] = fa(fm(fm(S1, q0), q1), fm(fm(S2, q2), q3));
   } else {
     s1 = sqrtf(a);
     s2 = sqrtf(c);
-    S1 = (ainv * s1 > 1.f) ? 1.f / (ainv * s1) : 1.f;
-    S2 = (ainv * s2 > 1.f) ? 1.f / (ainv * s2) : 1.f;
+    S1 = (fm(ainv, s1) > 1.f) ? 1.f / fm(ainv, s1) : 1.f;
+    S2 = (fm(ainv, s2) > 1.f) ? 1.f / fm(ainv, s2) : 1.f;
     M[0] = S1; M[2] = S2; M[1] = 0.f;
   }
 }
@@ -58,16 +70,16 @@ __device__ __forceinline__ void nucl2d_matrix(float a, float b, float c, float a
 // nuclear 3-D helpers (radon_tgv_primal_dual_3d.py:190-284), results by value
 __device__ __forceinline__ void diag2d(float a, float b, float c, float X[6]) {
   const float eps = 0.001f;
-  const float o = fminf(a, c);
-  if ((b * b) / (o * o) > eps && o * o > 0.f) {
-    const float dd = a + c, e = a - c;
-    float f = 4.f * b * b + e * e;
+  const float o = c < a ? c : a;
+  if (fm(b, b) / fm(o, o) > eps && fm(o, o) > 0.f) {
+    const float dd = fa(a, c), e = fs(a, c);
+    float f = fa(fm(fm(4.f, b), b), fm(e, e));
     f = f < 0.f ? 0.f : sqrtf(f);
-    X[1] = (dd - f > 0.f) ? (dd - f) * 0.5f : 0.f;
-    X[0] = (dd + f > 0.f) ? (dd + f) * 0.5f : 0.f;
-    const float h = (e - f) * 0.5f;
+    X[1] = (fs(dd, f) > 0.f) ? fm(fs(dd, f), 0.5f) : 0.f;
+    X[0] = (fa(dd, f) > 0.f) ? fm(fa(dd, f), 0.5f) : 0.f;
+    const float h = fm(fs(e, f), 0.5f);
     float v0 = 1.f, v1 = -h / b;
-    const float n1 = hypotf(v0, v1);
+    const float n1 = hyp(v0, v1);
     v0 = v0 / n1; v1 = v1 / n1;
     X[2] = v0; X[3] = v1; X[4] = v1; X[5] = -v0;
   } else {
@@ -76,37 +88,45 @@ __device__ __forceinline__ void diag2d(float a, float b, float c, float X[6]) {
 }
 
 __device__ __forceinline__ void eig3d(float a, float b, float c, float d, float e, float f, float out[3]) {
-  const float pi = 3.14159265359f;
-  float c2 = -(a + b + c);
-  const float c1 = a * b + a * c + b * c - d * d - e * e - f * f;
-  const float c0 = a * f * f + b * e * e + c * d * d - a * b * c - 2.f * d * e * f;
-  float p = (float)((double)(c2 * c2) - 3.0 * (double)c1);
-  const float q = -13.5f * c0 - c2 * c2 * c2 + 4.5f * c2 * c1;
-  float phi = (1.f / 3.f) * atanf(sqrtf(27.f * (0.25f * c1 * c1 * (p - c1) + c0 * (q + 6.75f * c0))) / q);
-  if (q < 0.f) phi += pi / 3.f;
-  const float x1 = 2.f * cosf(phi), x2 = 2.f * cosf(phi + 2.f * pi / 3.f), x3 = 2.f * cosf(phi - 2.f * pi / 3.f);
+  const float pi = (float)3.14159265359;
+  float c2 = -fa(fa(a, b), c);
+  const float c1 = fs(fs(fs(fa(fa(fm(a, b), fm(a, c)), fm(b, c)), fm(d, d)), fm(e, e)), fm(f, f));
+  const float c0 = fs(fs(fa(fa(fm(fm(a, f), f), fm(fm(b, e), e)), fm(fm(c, d), d)), fm(fm(a, b), c)),
+                      fm(fm(fm(2.f, d), e), f));
+  float p = (float)((double)fm(c2, c2) - 3.0 * (double)c1);
+  const float cube = (float)((double)c2 * c2 * c2);
+  const float q = fa(fs(fm(-13.5f, c0), cube), fm(fm(4.5f, c2), c1));
+  const float inner = fm(27.f, fa(fm(fm(fm(0.25f, c1), c1), fs(p, c1)), fm(c0, fa(q, fm(6.75f, c0)))));
+  float phi = fm(1.f / 3.f, (float)atan((double)(sqrtf(inner) / q)));
+  if (q < 0.f) phi = fa(phi, pi / 3.f);
+  const float x1 = fm(2.f, (float)cos((double)phi));
+  const float x2 = fm(2.f, (float)cos((double)fa(phi, fm(2.f, pi) / 3.f)));
+  const float x3 = fm(2.f, (float)cos((double)fs(phi, fm(2.f, pi) / 3.f)));
   p = sqrtf(p) / 3.f;
   c2 = c2 / 3.f;
-  out[0] = p * x1 - c2; out[1] = p * x2 - c2; out[2] = p * x3 - c2;
+  out[0] = fs(fm(p, x1), c2); out[1] = fs(fm(p, x2), c2); out[2] = fs(fm(p, x3), c2);
 }
 
 __device__ __forceinline__ void cross3(float a1, float a2, float a3, float b1, float b2, float b3, float o[3]) {
-  o[0] = a2 * b3 - a3 * b2;
-  o[1] = b1 * a3 - a1 * b3;
-  o[2] = a1 * b2 - a2 * b1;
+  o[0] = fs(fm(a2, b3), fm(a3, b2));
+  o[1] = fs(fm(b1, a3), fm(a1, b3));
+  o[2] = fs(fm(a1, b2), fm(a2, b1));
 }
 
+__device__ __forceinline__ float norm3(const float v[3]) { return sqrtf(fa(fa(fm(v[0], v[0]), fm(v[1], v[1])), fm(v[2], v[2]))); }
+
 // nuclear 3-D (update_NormV_Nucl, radon_tgv_primal_dual_3d.py:290-520): returns the
-// symmetric 3x3 projection matrix M (xx, yy, zz, xy, xz, yz) applied to every channel.
+// symmetric 3x3 projection matrix M (xx, yy, zz, xy, xz, yz) applied to every channel,
+// for A^T A = [a r t; r b d; t d c].
 __device__ void nucl3d_matrix(float a, float b, float c, float r, float t, float d, float ainv, float M[6]) {
   const float epsdt = 0.0001f, epsr = 0.0001f, epsoo = 0.0001f / ainv;
-  const float ndt = d * d + t * t;
-  float oo = fminf(a, b);
+  const float ndt = fa(fm(d, d), fm(t, t));
+  float oo = b < a ? b : a;
   float sig[3], v0[3], v1[3], v2[3], X[6], u1 = 1.f, u2 = 0.f;
-  if (ndt < epsdt * oo * oo && oo > epsoo) {
+  if (ndt < fm(fm(epsdt, oo), oo) && oo > epsoo) {
     diag2d(a, r, b, X);
     sig[0] = X[0]; sig[1] = X[1];
-    sig[2] = (c * c < ndt) ? 1.f / epsdt : c;
+    sig[2] = (fm(c, c) < ndt) ? 1.f / epsdt : c;
     v0[0] = X[2]; v0[1] = X[3]; v0[2] = 0.f;
     v1[0] = X[4]; v1[1] = X[5]; v1[2] = 0.f;
     v2[0] = 0.f; v2[1] = 0.f; v2[2] = 1.f;
@@ -125,16 +145,16 @@ __device__ void nucl3d_matrix(float a, float b, float c, float r, float t, float
       v2[0] = 0.f; v2[1] = X[4]; v2[2] = X[5];
     }
   } else {
-    const float t1 = b * t - d * r, t2 = a * d - t * r;
-    const float rs = sqrtf(ndt);
-    u1 = d / rs;
-    u2 = t / rs;
-    const float bn = (d * (b * d + r * t) + t * (a * t + d * r)) / ndt;
-    const float an = (t * t1 + d * t2) / ndt;
-    const float rn = (-d * t1 + t * t2) / ndt;
-    const float dn = rs;
-    oo = fminf(c, bn);
-    if (fabsf(rn) < epsr * oo) {
+    // rotate about z so that the (x, z) entry vanishes (3-D :434-452)
+    const float t1 = fs(fm(b, t), fm(d, r)), t2 = fs(fm(a, d), fm(t, r));
+    u1 = d / sqrtf(ndt);
+    u2 = t / sqrtf(ndt);
+    const float bn = fa(fm(d, fa(fm(b, d), fm(r, t))), fm(t, fa(fm(a, t), fm(d, r)))) / ndt;
+    const float an = fa(fm(t, t1), fm(d, t2)) / ndt;
+    const float rn = fa(fm(-d, t1), fm(t, t2)) / ndt;
+    const float dn = sqrtf(ndt);
+    oo = bn < c ? bn : c;
+    if (fabsf(rn) < fm(epsr, oo)) {
       diag2d(bn, dn, c, X);
       sig[0] = an; sig[1] = X[0]; sig[2] = X[1];
       v0[0] = 1.f; v0[1] = 0.f; v0[2] = 0.f;
@@ -142,37 +162,38 @@ __device__ void nucl3d_matrix(float a, float b, float c, float r, float t, float
       v2[0] = 0.f; v2[1] = X[4]; v2[2] = X[5];
     } else {
       eig3d(an, bn, c, rn, 0.f, dn, sig);
-      cross3(an - sig[0], rn, 0.f, rn, bn - sig[0], dn, v0);
-      float n = sqrtf(v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2]);
+      cross3(fs(an, sig[0]), rn, 0.f, rn, fs(bn, sig[0]), dn, v0);
+      float n = norm3(v0);
       v0[0] /= n; v0[1] /= n; v0[2] /= n;
-      cross3(v0[0], v0[1], v0[2], 0.f, dn, c - sig[1], v1);
-      n = sqrtf(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+      cross3(v0[0], v0[1], v0[2], 0.f, dn, fs(c, sig[1]), v1);
+      n = norm3(v1);
       v1[0] /= n; v1[1] /= n; v1[2] /= n;
       cross3(v0[0], v0[1], v0[2], v1[0], v1[1], v1[2], v2);
-      n = sqrtf(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+      n = norm3(v2);
       v2[0] /= n; v2[1] /= n; v2[2] /= n;
     }
   }
+  // eigenvectors back in the original frame (:476-479)
   float w[3][3];
-  const float *vv[3] = {v0, v1, v2};
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
-    w[m][0] = u1 * vv[m][0] + u2 * vv[m][1];
-    w[m][1] = -u2 * vv[m][0] + u1 * vv[m][1];
-    w[m][2] = vv[m][2];
+    const float *vv = m == 0 ? v0 : (m == 1 ? v1 : v2);
+    w[m][0] = fa(fm(u1, vv[0]), fm(u2, vv[1]));
+    w[m][1] = fa(fm(-u2, vv[0]), fm(u1, vv[1]));
+    w[m][2] = vv[2];
   }
   float S[3];
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
     const float sg = sig[m] > 0.f ? sqrtf(sig[m]) : 0.f;
-    S[m] = (sg * ainv > 1.f) ? 1.f / (ainv * sg) : 1.f;
+    S[m] = (fm(sg, ainv) > 1.f) ? 1.f / fm(ainv, sg) : 1.f;
   }
-  M[0] = S[0] * w[0][0] * w[0][0] + S[1] * w[1][0] * w[1][0] + S[2] * w[2][0] * w[2][0];
-  M[1] = S[0] * w[0][1] * w[0][1] + S[1] * w[1][1] * w[1][1] + S[2] * w[2][1] * w[2][1];
-  M[2] = S[0] * w[0][2] * w[0][2] + S[1] * w[1][2] * w[1][2] + S[2] * w[2][2] * w[2][2];
-  M[3] = S[0] * w[0][0] * w[0][1] + S[1] * w[1][0] * w[1][1] + S[2] * w[2][0] * w[2][1];
-  M[4] = S[0] * w[0][0] * w[0][2] + S[1] * w[1][0] * w[1][2] + S[2] * w[2][0] * w[2][2];
-  M[5] = S[0] * w[0][1] * w[0][2] + S[1] * w[1][1] * w[1][2] + S[2] * w[2][1] * w[2][2];
+  // M = W diag(S) W^T (:500-507)
+  const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int q = 0; q < 6; ++q)
+    M[q] = fa(fa(fm(fm(S[0], w[0][ii[q]]), w[0][jj[q]]), fm(fm(S[1], w[1][ii[q]]), w[1][jj[q]])),
+              fm(fm(S[2], w[2][ii[q]]), w[2][jj[q]]));
 }
 
 // squared norm of one channel's w in the reference's weighting:
@@ -298,7 +319,7 @@ __global__ void __launch_bounds__(256) k_dual(const IterParams P) {
 #pragma unroll
         for (int c = 0; c < CMAX; ++c) {
           if (c >= nC) break;
-          a += vv[c][0] * vv[c][0]; b += vv[c][0] * vv[c][1]; cc += vv[c][1] * vv[c][1];
+          a = fa(a, fm(vv[c][0], vv[c][0])); b = fa(b, fm(vv[c][0], vv[c][1])); cc = fa(cc, fm(vv[c][1], vv[c][1]));
         }
         float M[3];
         nucl2d_matrix(a, b, cc, P.ainv1, M);
@@ -306,8 +327,8 @@ __global__ void __launch_bounds__(256) k_dual(const IterParams P) {
         for (int c = 0; c < CMAX; ++c) {
           if (c >= nC) break;
           const float v0 = vv[c][0], v1 = vv[c][1];
-          vv[c][0] = v0 * M[0] + v1 * M[1];
-          vv[c][1] = v0 * M[1] + v1 * M[2];
+          vv[c][0] = fa(fm(v0, M[0]), fm(v1, M[1]));
+          vv[c][1] = fa(fm(v0, M[1]), fm(v1, M[2]));
         }
       } else {
         float a = 0.f, b = 0.f, cc = 0.f, r = 0.f, tt = 0.f, dd = 0.f;
@@ -315,7 +336,8 @@ __global__ void __launch_bounds__(256) k_dual(const IterParams P) {
         for (int c = 0; c < CMAX; ++c) {
           if (c >= nC) break;
           const float X = vv[c][0], Y = vv[c][1], Z = vv[c][DIM - 1];
-          a += X * X; b += Y * Y; cc += Z * Z; r += X * Y; tt += X * Z; dd += Y * Z;
+          a = fa(a, fm(X, X)); b = fa(b, fm(Y, Y)); cc = fa(cc, fm(Z, Z));
+          r = fa(r, fm(X, Y)); tt = fa(tt, fm(X, Z)); dd = fa(dd, fm(Y, Z));
         }
         float M[6];
         nucl3d_matrix(a, b, cc, r, tt, dd, P.ainv1, M);
@@ -323,9 +345,9 @@ __global__ void __launch_bounds__(256) k_dual(const IterParams P) {
         for (int c = 0; c < CMAX; ++c) {
           if (c >= nC) break;
           const float A = vv[c][0], B = vv[c][1], Cc = vv[c][DIM - 1];
-          vv[c][0] = A * M[0] + B * M[3] + Cc * M[4];
-          vv[c][1] = A * M[3] + B * M[1] + Cc * M[5];
-          vv[c][DIM - 1] = A * M[4] + B * M[5] + Cc * M[2];
+          vv[c][0] = fa(fa(fm(A, M[0]), fm(B, M[3])), fm(Cc, M[4]));
+          vv[c][1] = fa(fa(fm(A, M[3]), fm(B, M[1])), fm(Cc, M[5]));
+          vv[c][DIM - 1] = fa(fa(fm(A, M[4]), fm(B, M[5])), fm(Cc, M[2]));
         }
       }
     }
@@ -363,6 +385,53 @@ __global__ void __launch_bounds__(256) k_dual(const IterParams P) {
 }
 
 // ===========================================================================
+// vector access: a lane owns VW consecutive slices s0..s0+VW-1 (VW = 4, 2, 1
+// as S allows), so the per-pixel geometry of the projectors is computed once
+// per VW slices; every per-slice operation keeps the reference's order.
+// ===========================================================================
+template <int VW> __device__ __forceinline__ void ldv(const float *p, float (&r)[VW]);
+template <> __device__ __forceinline__ void ldv<4>(const float *p, float (&r)[4]) {
+  const float4 q = __ldg(reinterpret_cast<const float4 *>(p));
+  r[0] = q.x; r[1] = q.y; r[2] = q.z; r[3] = q.w;
+}
+template <> __device__ __forceinline__ void ldv<2>(const float *p, float (&r)[2]) {
+  const float2 q = __ldg(reinterpret_cast<const float2 *>(p));
+  r[0] = q.x; r[1] = q.y;
+}
+template <> __device__ __forceinline__ void ldv<1>(const float *p, float (&r)[1]) { r[0] = __ldg(p); }
+template <> __device__ __forceinline__ void ldv<8>(const float *p, float (&r)[8]) {
+  const float4 q0 = __ldg(reinterpret_cast<const float4 *>(p));
+  const float4 q1 = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+  r[0] = q0.x; r[1] = q0.y; r[2] = q0.z; r[3] = q0.w;
+  r[4] = q1.x; r[5] = q1.y; r[6] = q1.z; r[7] = q1.w;
+}
+
+// plain (coherent) loads for fields the same kernel also writes
+template <int VW> __device__ __forceinline__ void ldw(const float *p, float (&r)[VW]) {
+  if (VW == 8) {
+    const float4 q0 = reinterpret_cast<const float4 *>(p)[0], q1 = reinterpret_cast<const float4 *>(p)[1];
+    r[0] = q0.x; r[1] = q0.y; r[2] = q0.z; r[3] = q0.w;
+    r[4 % VW] = q1.x; r[5 % VW] = q1.y; r[6 % VW] = q1.z; r[7 % VW] = q1.w;
+  } else if (VW == 4) {
+    const float4 q = *reinterpret_cast<const float4 *>(p);
+    r[0] = q.x; r[1 % VW] = q.y; r[2 % VW] = q.z; r[3 % VW] = q.w;
+  } else if (VW == 2) {
+    const float2 q = *reinterpret_cast<const float2 *>(p);
+    r[0] = q.x; r[1 % VW] = q.y;
+  } else {
+    r[0] = p[0];
+  }
+}
+template <int VW> __device__ __forceinline__ void stv(float *p, const float (&r)[VW]) {
+  if (VW == 8) {
+    reinterpret_cast<float4 *>(p)[0] = make_float4(r[0], r[1], r[2], r[3]);
+    reinterpret_cast<float4 *>(p)[1] = make_float4(r[4 % VW], r[5 % VW], r[6 % VW], r[7 % VW]);
+  } else if (VW == 4) *reinterpret_cast<float4 *>(p) = make_float4(r[0], r[1 % VW], r[2 % VW], r[3 % VW]);
+  else if (VW == 2) *reinterpret_cast<float2 *>(p) = make_float2(r[0], r[1 % VW]);
+  else p[0] = r[0];
+}
+
+// ===========================================================================
 // forward projection: kernel `radon` (3-D :773-816).  Ray (i, j) of slice s:
 // acc = sum over rows y and x in [x_low, x_high] of (1 - |x X + y Y + off - i|)+ img.
 // The arithmetic is the reference's, in its order and without contraction.
@@ -388,11 +457,14 @@ __device__ __forceinline__ void ray_rows(const float4 o, int i, int N, int &ylo,
   yhi = min(N - 1, (int)ceilf(yb) + 1);
 }
 
-__device__ __forceinline__ float radon_ray(const float *__restrict__ img, size_t S, int N, const float4 o, int i) {
+template <int VW>
+__device__ __forceinline__ void radon_ray(const float *__restrict__ img, size_t S, int N, const float4 o, int i,
+                                          float (&acc)[VW]) {
   int ylo, yhi;
   ray_rows(o, i, N, ylo, yhi);
   const float fi = (float)i, fim = (float)(i - 1), fip = (float)(i + 1);
-  float acc = 0.f;
+#pragma unroll
+  for (int k = 0; k < VW; ++k) acc[k] = 0.f;
   for (int y = ylo; y <= yhi; ++y) {
     const float d = __fadd_rn(__fmul_rn((float)y, o.y), o.z);
     int xl, xh;
@@ -410,157 +482,231 @@ __device__ __forceinline__ float radon_ray(const float *__restrict__ img, size_t
     const float *row = img + (size_t)y * N * S;
     for (int x = xl; x <= xh; ++x) {
       const float wgt = 1.0f - fabsf(__fsub_rn(__fadd_rn(__fmul_rn((float)x, o.x), d), fi));
-      if (wgt > 0.f) acc = __fadd_rn(acc, __fmul_rn(wgt, __ldg(row + (size_t)x * S)));
+      if (wgt > 0.f) {
+        float val[VW];
+        ldv<VW>(row + (size_t)x * S, val);
+#pragma unroll
+        for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(wgt, val[k]));
+      }
     }
   }
-  return acc;
 }
 
 // k_fwd: radon of ubar fused with update_lambda_KL (3-D :690-704) or _L2 (:677-688).
-template <int DISC>
+// thread = one (bin, slice group of VW).
+template <int DISC, int VW>
 __global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
   const Dims d = P.d;
+  const int nsg = d.S / VW;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)d.nbin) return;
-  const int b = (int)(t / d.S);
-  const int s = (int)(t - (long long)b * d.S);
+  if (t >= (long long)d.nd * d.nang * nsg) return;
+  const int b = (int)(t / nsg);
+  const int s0 = (int)(t - (long long)b * nsg) * VW;
   const int j = b / d.nd, i = b - j * d.nd;
   const float4 o = __ldg(P.ofs + j);
-  const float acc = radon_ray(P.ubar + s, d.S, d.N, o, i);
-  const size_t q = (size_t)t;
-  P.ku[q] = acc;
-  const float m = __ldg(P.mu + s / d.Nz);
+  float acc[VW];
+  radon_ray<VW>(P.ubar + s0, d.S, d.N, o, i, acc);
+  const size_t q = (size_t)b * d.S + s0;
+  stv<VW>(P.ku + q, acc);
+  float lam[VW], f[VW];
+  ldw<VW>(P.lam + q, lam);
+  ldv<VW>(P.f + q, f);
   const float sd = P.sigma_data;
-  float lam = P.lam[q];
-  if (DISC == KL) {
-    const float sv = lam + sd * acc;
-    const float wv = sv - m;
-    const float dv = wv * wv + 4.f * sd * P.f[q] * m;
-    lam = sv - 0.5f * (wv + sqrtf(dv));
-  } else {
-    lam = (lam + sd * (acc - P.f[q])) * m;
+#pragma unroll
+  for (int k = 0; k < VW; ++k) {
+    const float m = __ldg(P.mu + (s0 + k) / d.Nz);
+    if (DISC == KL) {
+      const float sv = lam[k] + sd * acc[k];
+      const float wv = sv - m;
+      const float dv = wv * wv + 4.f * sd * f[k] * m;
+      lam[k] = sv - 0.5f * (wv + sqrtf(dv));
+    } else {
+      lam[k] = (lam[k] + sd * (acc[k] - f[k])) * m;
+    }
   }
-  P.lam[q] = lam;
+  stv<VW>(P.lam + q, lam);
 }
 
 // ===========================================================================
 // back projection: kernel `radon_ad` (3-D :818-844): linear interpolation
 // between detector bins floor(t) and floor(t)+1 at t = dot((x, y, 1, 0), ofs[j]).
 // ===========================================================================
-__device__ __forceinline__ float radon_ad_pixel(const float *__restrict__ lam, size_t S, int nd, int nang,
-                                                const float4 *__restrict__ ofs, float xf, float yf) {
-  float acc = 0.f;
+template <int VW>
+__device__ __forceinline__ void radon_ad_pixel(const float *__restrict__ lam, size_t S, int nd, int nang,
+                                               const float4 *__restrict__ ofs, float xf, float yf, float (&acc)[VW]) {
+#pragma unroll
+  for (int k = 0; k < VW; ++k) acc[k] = 0.f;
   const float fnd = (float)nd;
+#pragma unroll 2
   for (int j = 0; j < nang; ++j) {
     const float4 o = __ldg(ofs + j);
     const float tt = __fadd_rn(__fadd_rn(__fmul_rn(xf, o.x), __fmul_rn(yf, o.y)), o.z);
     if (tt > -1.f && tt < fnd) {
       const float fl = floorf(tt);
       const float p = fminf(__fsub_rn(tt, fl), 0x1.fffffep-1f);
+      const float q = __fsub_rn(1.0f, p);
       const int il = (int)fl;
       const float *lj = lam + (size_t)j * nd * S;
-      if (il >= 0) acc = __fadd_rn(acc, __fmul_rn(__fsub_rn(1.0f, p), __ldg(lj + (size_t)il * S)));
-      if (il <= nd - 2) acc = __fadd_rn(acc, __fmul_rn(p, __ldg(lj + (size_t)(il + 1) * S)));
+      float a[VW], b[VW];
+      if (il >= 0) {
+        ldv<VW>(lj + (size_t)il * S, a);
+#pragma unroll
+        for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(q, a[k]));
+      }
+      if (il <= nd - 2) {
+        ldv<VW>(lj + (size_t)(il + 1) * S, b);
+#pragma unroll
+        for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(p, b[k]));
+      }
     }
   }
-  return acc;
 }
 
 // k_primal: radon_ad of lambda + update_u (3-D :706-729, 2-D :340-357) +
 // update_p (3-D :734-757, 2-D :359-376) + extrapolation and swap (:1217-1221).
-// thread = one (pixel, s).
-template <int DIM, bool TGV>
+// thread = one (pixel, slice group of VW).
+template <int DIM, bool TGV, int UW>
+__device__ __forceinline__ void primal_update(const IterParams &P, int x, int y, int s0, const float (&kstar)[UW]);
+
+template <int DIM, bool TGV, int VW>
 __global__ void __launch_bounds__(256) k_primal(const IterParams P) {
   const Dims d = P.d;
+  const int nsg = d.S / VW;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)d.vol) return;
-  const int pix = (int)(t / d.S);
-  const int s = (int)(t - (long long)pix * d.S);
+  if (t >= (long long)d.N * d.N * nsg) return;
+  const int pix = (int)(t / nsg);
+  const int s0 = (int)(t - (long long)pix * nsg) * VW;
   const int y = pix / d.N, x = pix - y * d.N;
-  const int z = (DIM == 3) ? s % d.Nz : 0;
-  const size_t S = d.S, rowS = (size_t)d.N * S, vol = d.vol, i = (size_t)t;
+  float kstar[VW];
+  radon_ad_pixel<VW>(P.lam + s0, d.S, d.nd, d.nang, P.ofs, (float)x, (float)y, kstar);
+  // the memory-bound update part works on at most 4 slices at a time (registers)
+  constexpr int UW = VW > 4 ? 4 : VW;
+#pragma unroll
+  for (int h = 0; h < VW / UW; ++h) {
+    float ks[UW];
+#pragma unroll
+    for (int k = 0; k < UW; ++k) ks[k] = kstar[h * UW + k];
+    primal_update<DIM, TGV, UW>(P, x, y, s0 + h * UW, ks);
+  }
+}
 
-  const float kstar = radon_ad_pixel(P.lam + s, S, d.nd, d.nang, P.ofs, (float)x, (float)y);
+template <int DIM, bool TGV, int VW>
+__device__ __forceinline__ void primal_update(const IterParams &P, int x, int y, int s0, const float (&kstar)[VW]) {
+  const Dims d = P.d;
+  const size_t S = d.S, rowS = (size_t)d.N * S, vol = d.vol, i = ((size_t)y * d.N + x) * S + s0;
+  int z[VW];
+#pragma unroll
+  for (int k = 0; k < VW; ++k) z[k] = (DIM == 3) ? (s0 + k) % d.Nz : 0;
 
   // divergence of v: backward differences (adjoint of the forward gradient)
   const float *__restrict__ v = P.v;
-  float a = v[i], b = v[vol + i];
-  if (x == d.N - 1) a = 0.f;
-  if (x > 0) a -= v[i - S];
-  if (y == d.N - 1) b = 0.f;
-  if (y > 0) b -= v[vol + i - rowS];
-  const float uo = P.u[i];
-  float un;
+  float a[VW], b[VW], am[VW], bm[VW], uo[VW], un[VW], ub[VW];
+  ldw<VW>(v + i, a);
+  ldw<VW>(v + vol + i, b);
+  if (x > 0) ldw<VW>(v + i - S, am);
+  if (y > 0) ldw<VW>(v + vol + i - rowS, bm);
+  ldw<VW>(P.u + i, uo);
+  float c[VW], cprev = 0.f;
   if (DIM == 3) {
-    float c = v[2 * vol + i];
-    if (z == d.Nz - 1) c = 0.f;
-    if (z > 0) c -= v[2 * vol + i - 1];
-    c /= P.stepsize;
-    un = uo + P.tau * (a + b + c - P.norming * kstar);
-  } else {
-    un = uo + P.tau * (a + b - P.norming * kstar);
+    ldw<VW>(v + 2 * vol + i, c);
+    if (z[0] > 0) cprev = v[2 * vol + i - 1];
   }
-  if (un < 0.f) un = 0.f;
-  P.ubar[i] = 2.0f * un - uo;
-  P.u[i] = un;
+#pragma unroll
+  for (int k = 0; k < VW; ++k) {
+    float ak = a[k], bk = b[k];
+    if (x == d.N - 1) ak = 0.f;
+    if (x > 0) ak -= am[k];
+    if (y == d.N - 1) bk = 0.f;
+    if (y > 0) bk -= bm[k];
+    float r;
+    if (DIM == 3) {
+      float ck = c[k];
+      if (z[k] == d.Nz - 1) ck = 0.f;
+      if (z[k] > 0) ck -= (k > 0 ? c[k - 1] : cprev);
+      ck /= P.stepsize;
+      r = uo[k] + P.tau * (ak + bk + ck - P.norming * kstar[k]);
+    } else {
+      r = uo[k] + P.tau * (ak + bk - P.norming * kstar[k]);
+    }
+    if (r < 0.f) r = 0.f;
+    un[k] = r;
+    ub[k] = 2.0f * r - uo[k];
+  }
+  stv<VW>(P.ubar + i, ub);
+  stv<VW>(P.u + i, un);
 
   if (TGV) {
     const float *__restrict__ w = P.w;
-    if (DIM == 3) {
-      // rows of the symmetric tensor: (w0 w3 w4), (w3 w1 w5), (w4 w5 w2)
-      const int rx[3] = {0, 3, 4}, ry[3] = {3, 1, 5}, rz[3] = {4, 5, 2};
+    constexpr int K = DIM;
+    // rows of the symmetric tensor: 3-D (w0 w3 w4), (w3 w1 w5), (w4 w5 w2); 2-D (w0 w2), (w2 w1)
+    const int rx[3] = {0, DIM == 3 ? 3 : 2, 4}, ry[3] = {DIM == 3 ? 3 : 2, 1, 5}, rz[3] = {4, 5, 2};
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        float A = -w[rx[k] * vol + i], B = -w[ry[k] * vol + i], Cz = -w[rz[k] * vol + i];
-        if (x == 0) A = 0.f;
-        if (x < d.N - 1) A += w[rx[k] * vol + i + S];
-        if (y == 0) B = 0.f;
-        if (y < d.N - 1) B += w[ry[k] * vol + i + rowS];
-        if (z == 0) Cz = 0.f;
-        if (z < d.Nz - 1) Cz += w[rz[k] * vol + i + 1];
-        Cz /= P.stepsize;
-        const float po = P.p[k * vol + i];
-        const float pn = po + P.tau * (v[k * vol + i] + A + B + Cz);
-        P.pbar[k * vol + i] = 2.0f * pn - po;
-        P.p[k * vol + i] = pn;
+    for (int k = 0; k < K; ++k) {
+      float wa[VW], wan[VW], wb[VW], wbn[VW], po[VW], vk[VW], pn[VW], pb[VW];
+      ldw<VW>(w + rx[k] * vol + i, wa);
+      ldw<VW>(w + ry[k] * vol + i, wb);
+      if (x < d.N - 1) ldw<VW>(w + rx[k] * vol + i + S, wan);
+      if (y < d.N - 1) ldw<VW>(w + ry[k] * vol + i + rowS, wbn);
+      ldw<VW>(P.p + k * vol + i, po);
+      ldw<VW>(v + k * vol + i, vk);
+      float wc[VW], wcnext = 0.f;
+      if (DIM == 3) {
+        ldw<VW>(w + rz[k] * vol + i, wc);
+        if (z[VW - 1] < d.Nz - 1) wcnext = w[rz[k] * vol + i + VW];
       }
-    } else {
-      const int rx[2] = {0, 2}, ry[2] = {2, 1};
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        float A = -w[rx[k] * vol + i], B = -w[ry[k] * vol + i];
+      for (int e = 0; e < VW; ++e) {
+        float A = -wa[e], B = -wb[e];
         if (x == 0) A = 0.f;
-        if (x < d.N - 1) A += w[rx[k] * vol + i + S];
+        if (x < d.N - 1) A += wan[e];
         if (y == 0) B = 0.f;
-        if (y < d.N - 1) B += w[ry[k] * vol + i + rowS];
-        const float po = P.p[k * vol + i];
-        const float pn = po + P.tau * (v[k * vol + i] + A + B);
-        P.pbar[k * vol + i] = 2.0f * pn - po;
-        P.p[k * vol + i] = pn;
+        if (y < d.N - 1) B += wbn[e];
+        float r;
+        if (DIM == 3) {
+          float Cz = -wc[e];
+          if (z[e] == 0) Cz = 0.f;
+          if (z[e] < d.Nz - 1) Cz += (e < VW - 1 ? wc[e + 1] : wcnext);
+          Cz /= P.stepsize;
+          r = po[e] + P.tau * (vk[e] + A + B + Cz);
+        } else {
+          r = po[e] + P.tau * (vk[e] + A + B);
+        }
+        pn[e] = r;
+        pb[e] = 2.0f * r - po[e];
       }
+      stv<VW>(P.pbar + k * vol + i, pb);
+      stv<VW>(P.p + k * vol + i, pn);
     }
   }
 }
 
 // ===========================================================================
-// standalone projectors and layout transposes
+// standalone projectors
 // ===========================================================================
+template <int VW>
 __global__ void k_radon(const float *__restrict__ img, float *__restrict__ sino, const float4 *__restrict__ ofs,
                         int N, int nd, int nang, int S) {
+  const int nsg = S / VW;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nd * nang * S) return;
-  const int b = (int)(t / S), s = (int)(t - (long long)b * S);
+  if (t >= (long long)nd * nang * nsg) return;
+  const int b = (int)(t / nsg), s0 = (int)(t - (long long)b * nsg) * VW;
   const int j = b / nd, i = b - j * nd;
-  sino[t] = radon_ray(img + s, S, N, __ldg(ofs + j), i);
+  float acc[VW];
+  radon_ray<VW>(img + s0, S, N, __ldg(ofs + j), i, acc);
+  stv<VW>(sino + (size_t)b * S + s0, acc);
 }
 
+template <int VW>
 __global__ void k_radon_ad(const float *__restrict__ sino, float *__restrict__ img, const float4 *__restrict__ ofs,
                            int N, int nd, int nang, int S) {
+  const int nsg = S / VW;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)N * N * S) return;
-  const int pix = (int)(t / S), s = (int)(t - (long long)pix * S);
+  if (t >= (long long)N * N * nsg) return;
+  const int pix = (int)(t / nsg), s0 = (int)(t - (long long)pix * nsg) * VW;
   const int y = pix / N, x = pix - y * N;
-  img[t] = radon_ad_pixel(sino + s, S, nd, nang, ofs, (float)x, (float)y);
+  float acc[VW];
+  radon_ad_pixel<VW>(sino + s0, S, nd, nang, ofs, (float)x, (float)y, acc);
+  stv<VW>(img + (size_t)pix * S + s0, acc);
 }
 
 // out[c][r] = in[r][c]: host layout [S][X] <-> device layout [X][S], 32x32 tiles,
@@ -697,34 +843,67 @@ cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st) 
   return tgv ? launch_dual_t<2, true>(P, cpl, st) : launch_dual_t<2, false>(P, cpl, st);
 }
 
+// slices per lane: 4 when S allows aligned float4 access, else 2, else 1
+static inline int vec_width(int S) { return (S % 8 == 0) ? 8 : (S % 4 == 0) ? 4 : (S % 2 == 0 ? 2 : 1); }
+
+template <int VW>
+static void fwd_vw(const IterParams &P, int disc, cudaStream_t st) {
+  const unsigned g = blocks_for((long long)P.d.nd * P.d.nang * (P.d.S / VW), 256);
+  if (disc == KL) k_fwd<KL, VW><<<g, 256, 0, st>>>(P);
+  else k_fwd<L2, VW><<<g, 256, 0, st>>>(P);
+}
+
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
-  const unsigned g = blocks_for((long long)P.d.nbin, 256);
-  if (disc == KL) k_fwd<KL><<<g, 256, 0, st>>>(P);
-  else k_fwd<L2><<<g, 256, 0, st>>>(P);
+  const int vw = vec_width(P.d.S);
+  if (vw == 8) fwd_vw<8>(P, disc, st);
+  else if (vw == 4) fwd_vw<4>(P, disc, st);
+  else if (vw == 2) fwd_vw<2>(P, disc, st);
+  else fwd_vw<1>(P, disc, st);
   return cudaGetLastError();
+}
+
+template <int VW>
+static void primal_vw(const IterParams &P, int tgv, cudaStream_t st) {
+  const unsigned g = blocks_for((long long)P.d.N * P.d.N * (P.d.S / VW), 256);
+  if (P.d.dim == 3) {
+    if (tgv) k_primal<3, true, VW><<<g, 256, 0, st>>>(P);
+    else k_primal<3, false, VW><<<g, 256, 0, st>>>(P);
+  } else {
+    if (tgv) k_primal<2, true, VW><<<g, 256, 0, st>>>(P);
+    else k_primal<2, false, VW><<<g, 256, 0, st>>>(P);
+  }
 }
 
 cudaError_t launch_primal(const IterParams &P, int tgv, cudaStream_t st) {
-  const unsigned g = blocks_for((long long)P.d.vol, 256);
-  if (P.d.dim == 3) {
-    if (tgv) k_primal<3, true><<<g, 256, 0, st>>>(P);
-    else k_primal<3, false><<<g, 256, 0, st>>>(P);
-  } else {
-    if (tgv) k_primal<2, true><<<g, 256, 0, st>>>(P);
-    else k_primal<2, false><<<g, 256, 0, st>>>(P);
-  }
+  const int vw = vec_width(P.d.S);
+  if (vw == 8) primal_vw<8>(P, tgv, st);
+  else if (vw == 4) primal_vw<4>(P, tgv, st);
+  else if (vw == 2) primal_vw<2>(P, tgv, st);
+  else primal_vw<1>(P, tgv, st);
   return cudaGetLastError();
 }
 
+static inline bool aligned(const void *p, int vw) { return ((uintptr_t)p % (4 * vw)) == 0; }
+
 cudaError_t launch_radon(const float *img, float *sino, const float4 *ofs, int N, int nd, int nang, int S,
                          cudaStream_t st) {
-  k_radon<<<blocks_for((long long)nd * nang * S, 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
+  int vw = vec_width(S);
+  while (vw > 1 && !(aligned(img, vw > 4 ? 4 : vw) && aligned(sino, vw > 4 ? 4 : vw))) vw /= 2;
+  if (vw == 8) k_radon<8><<<blocks_for((long long)nd * nang * (S / 8), 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
+  else if (vw == 4) k_radon<4><<<blocks_for((long long)nd * nang * (S / 4), 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
+  else if (vw == 2) k_radon<2><<<blocks_for((long long)nd * nang * (S / 2), 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
+  else k_radon<1><<<blocks_for((long long)nd * nang * S, 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
   return cudaGetLastError();
 }
 
 cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, int N, int nd, int nang, int S,
                             cudaStream_t st) {
-  k_radon_ad<<<blocks_for((long long)N * N * S, 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
+  int vw = vec_width(S);
+  while (vw > 1 && !(aligned(img, vw > 4 ? 4 : vw) && aligned(sino, vw > 4 ? 4 : vw))) vw /= 2;
+  if (vw == 8) k_radon_ad<8><<<blocks_for((long long)N * N * (S / 8), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
+  else if (vw == 4) k_radon_ad<4><<<blocks_for((long long)N * N * (S / 4), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
+  else if (vw == 2) k_radon_ad<2><<<blocks_for((long long)N * N * (S / 2), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
+  else k_radon_ad<1><<<blocks_for((long long)N * N * S, 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
   return cudaGetLastError();
 }
 

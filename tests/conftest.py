@@ -26,3 +26,22 @@ def golden():
         return cache[name]
 
     return load
+
+
+_REPORT = []
+
+
+@pytest.fixture(scope="session")
+def parity_report():
+    """Collects (case, iterations, field, relative L2) rows; written as JSON lines to
+    $GRAPTOR_PARITY_REPORT at the end of the session when that variable is set."""
+    yield _REPORT.append
+
+
+def pytest_sessionfinish(session, exitstatus):
+    path = os.environ.get("GRAPTOR_PARITY_REPORT")
+    if path and _REPORT:
+        import json
+        with open(path, "w") as f:
+            for row in _REPORT:
+                f.write(json.dumps(row) + "\n")
