@@ -28,6 +28,9 @@ cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, dou
                       double *d_part, double *out, cudaStream_t st);
 cudaError_t fill_f64(double *x, size_t n, double v, cudaStream_t st);
 cudaError_t fill_f32(float *x, size_t n, float v, cudaStream_t st);
+cudaError_t launch_ray_count(const float4 *ofs, int N, int nd, int nang, int *count, cudaStream_t st);
+cudaError_t launch_ray_fill(const float4 *ofs, int N, int nd, int nang, const long long *start, int2 *ent,
+                            cudaStream_t st);
 }  // namespace gt
 
 namespace {
@@ -99,6 +102,8 @@ struct gt_problem {
   float *mu_eff = nullptr;
   float *u = nullptr, *ubar = nullptr, *p = nullptr, *pbar = nullptr, *v = nullptr, *w = nullptr;
   float *lam = nullptr, *f = nullptr, *ku = nullptr, *stage = nullptr;
+  void *rays = nullptr;        // ray table (offsets + entries), built at creation
+  size_t ray_bytes = 0;
   gt::IterParams P{};
   cudaGraphExec_t g_one = nullptr, g_chunk = nullptr;
   int chunk = 16;
@@ -279,6 +284,35 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
       (e = cudaStreamSynchronize(p->stream)) != cudaSuccess)
     return fail(cuda_err(e, "problem setup", __LINE__));
 
+  // ray table of the forward projector (entries of all rays, see k_ray_fill)
+  {
+    const int nr = D.nd * D.nang;
+    std::vector<int> cnt(nr);
+    std::vector<long long> start(nr + 1, 0);
+    int *d_cnt = (int *)p->stage;  // stage is free scratch now (>= nr floats)
+    if ((e = gt::launch_ray_count(p->ofs, D.N, D.nd, D.nang, d_cnt, p->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * nr, cudaMemcpyDeviceToHost, p->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(p->stream)) != cudaSuccess)
+      return fail(cuda_err(e, "ray table count", __LINE__));
+    for (int r = 0; r < nr; ++r) start[r + 1] = start[r] + cnt[r];
+    const size_t off_b = align256(sizeof(long long) * (nr + 1));
+    p->ray_bytes = off_b + sizeof(int2) * (size_t)start[nr];
+    if ((e = cudaMalloc(&p->rays, p->ray_bytes)) != cudaSuccess) {
+      cudaGetLastError();
+      gt_problem_destroy(p);
+      return set_err(GT_ERR_OOM, "ray table allocation of %.3f GB failed", p->ray_bytes / 1e9);
+    }
+    long long *d_start = (long long *)p->rays;
+    int2 *d_ent = (int2 *)((char *)p->rays + off_b);
+    if ((e = cudaMemcpyAsync(d_start, start.data(), sizeof(long long) * (nr + 1), cudaMemcpyHostToDevice,
+                             p->stream)) != cudaSuccess ||
+        (e = gt::launch_ray_fill(p->ofs, D.N, D.nd, D.nang, d_start, d_ent, p->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(p->stream)) != cudaSuccess)
+      return fail(cuda_err(e, "ray table fill", __LINE__));
+    p->P.ray_start = d_start;
+    p->P.ray_ent = d_ent;
+  }
+
   gt::IterParams &P = p->P;
   P.d = p->d;
   P.ofs = p->ofs; P.mu = p->mu_eff;
@@ -295,6 +329,7 @@ void gt_problem_destroy(gt_problem *p) {
   if (p->g_one) cudaGraphExecDestroy(p->g_one);
   if (p->g_chunk) cudaGraphExecDestroy(p->g_chunk);
   if (p->block) cudaFree(p->block);
+  if (p->rays) cudaFree(p->rays);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
   if (p->side) cudaStreamDestroy(p->side);

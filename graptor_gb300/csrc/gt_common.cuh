@@ -42,6 +42,8 @@ struct IterParams {
   float stepsize;
   int cbase;             // first channel handled by a k_dual launch (0 unless C > 8)
   const float4 *ofs;     // [nang] (X, Y, offset, Xinv)
+  const long long *ray_start;  // [nd*nang + 1] ray table offsets (null: walk rays on the fly)
+  const int2 *ray_ent;         // (pixel, weight bits) entries of all rays
   const float *mu;       // [C] mu (KL) or mu/(sigma+mu) (L2)
   float *u, *ubar;       // [vol]
   float *p, *pbar, *v;   // [K][vol]

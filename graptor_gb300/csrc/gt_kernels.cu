@@ -384,35 +384,9 @@ __global__ void __launch_bounds__(256) k_dual(const IterParams P) {
   }
 }
 
-// ===========================================================================
-// vector access: a lane owns VW consecutive slices s0..s0+VW-1 (VW = 4, 2, 1
-// as S allows), so the per-pixel geometry of the projectors is computed once
-// per VW slices; every per-slice operation keeps the reference's order.
-// ===========================================================================
-template <int VW> __device__ __forceinline__ void ldv(const float *p, float (&r)[VW]);
-template <> __device__ __forceinline__ void ldv<4>(const float *p, float (&r)[4]) {
-  const float4 q = __ldg(reinterpret_cast<const float4 *>(p));
-  r[0] = q.x; r[1] = q.y; r[2] = q.z; r[3] = q.w;
-}
-template <> __device__ __forceinline__ void ldv<2>(const float *p, float (&r)[2]) {
-  const float2 q = __ldg(reinterpret_cast<const float2 *>(p));
-  r[0] = q.x; r[1] = q.y;
-}
-template <> __device__ __forceinline__ void ldv<1>(const float *p, float (&r)[1]) { r[0] = __ldg(p); }
-template <> __device__ __forceinline__ void ldv<8>(const float *p, float (&r)[8]) {
-  const float4 q0 = __ldg(reinterpret_cast<const float4 *>(p));
-  const float4 q1 = __ldg(reinterpret_cast<const float4 *>(p) + 1);
-  r[0] = q0.x; r[1] = q0.y; r[2] = q0.z; r[3] = q0.w;
-  r[4] = q1.x; r[5] = q1.y; r[6] = q1.z; r[7] = q1.w;
-}
-
-// plain (coherent) loads for fields the same kernel also writes
+// coherent vector loads / stores of UW consecutive slices (fields a kernel also writes)
 template <int VW> __device__ __forceinline__ void ldw(const float *p, float (&r)[VW]) {
-  if (VW == 8) {
-    const float4 q0 = reinterpret_cast<const float4 *>(p)[0], q1 = reinterpret_cast<const float4 *>(p)[1];
-    r[0] = q0.x; r[1] = q0.y; r[2] = q0.z; r[3] = q0.w;
-    r[4 % VW] = q1.x; r[5 % VW] = q1.y; r[6 % VW] = q1.z; r[7 % VW] = q1.w;
-  } else if (VW == 4) {
+  if (VW == 4) {
     const float4 q = *reinterpret_cast<const float4 *>(p);
     r[0] = q.x; r[1 % VW] = q.y; r[2 % VW] = q.z; r[3 % VW] = q.w;
   } else if (VW == 2) {
@@ -423,12 +397,94 @@ template <int VW> __device__ __forceinline__ void ldw(const float *p, float (&r)
   }
 }
 template <int VW> __device__ __forceinline__ void stv(float *p, const float (&r)[VW]) {
-  if (VW == 8) {
-    reinterpret_cast<float4 *>(p)[0] = make_float4(r[0], r[1], r[2], r[3]);
-    reinterpret_cast<float4 *>(p)[1] = make_float4(r[4 % VW], r[5 % VW], r[6 % VW], r[7 % VW]);
-  } else if (VW == 4) *reinterpret_cast<float4 *>(p) = make_float4(r[0], r[1 % VW], r[2 % VW], r[3 % VW]);
+  if (VW == 4) *reinterpret_cast<float4 *>(p) = make_float4(r[0], r[1 % VW], r[2 % VW], r[3 % VW]);
   else if (VW == 2) *reinterpret_cast<float2 *>(p) = make_float2(r[0], r[1 % VW]);
   else p[0] = r[0];
+}
+
+// ===========================================================================
+// slice sets: a lane owns VW slices and the per-pixel geometry of the
+// projectors is computed once for them; every per-slice operation keeps the
+// reference's order.
+//   VW = 8: two float4 chunks, slices 4l..4l+3 and 128+4l..128+4l+3 of the warp's
+//           256-slice block (l = lane), so each load instruction of the warp
+//           reads 512 contiguous bytes; a warp never straddles pixels or bins.
+//   VW = 2, 1: VW consecutive slices per thread (S not a multiple of 4).
+// ===========================================================================
+template <int VW>
+struct Slices {
+  int s0;         // first slice of chunk a (VW = 8: chunk b starts at s0 + 128)
+  bool va, vb;    // chunk a / b inside [0, S)
+  __device__ __forceinline__ void load(const float *base, float (&r)[VW]) const {
+    if (VW == 8) {
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+      if (va) a = __ldg(reinterpret_cast<const float4 *>(base + s0));
+      if (vb) b = __ldg(reinterpret_cast<const float4 *>(base + s0 + 128));
+      r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+      r[4 % VW] = b.x; r[5 % VW] = b.y; r[6 % VW] = b.z; r[7 % VW] = b.w;
+    } else if (VW == 2) {
+      const float2 a = __ldg(reinterpret_cast<const float2 *>(base + s0));
+      r[0] = a.x; r[1 % VW] = a.y;
+    } else {
+      r[0] = __ldg(base + s0);
+    }
+  }
+  // coherent load (fields this kernel also writes)
+  __device__ __forceinline__ void loadw(const float *base, float (&r)[VW]) const {
+    if (VW == 8) {
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+      if (va) a = *reinterpret_cast<const float4 *>(base + s0);
+      if (vb) b = *reinterpret_cast<const float4 *>(base + s0 + 128);
+      r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+      r[4 % VW] = b.x; r[5 % VW] = b.y; r[6 % VW] = b.z; r[7 % VW] = b.w;
+    } else if (VW == 2) {
+      const float2 a = *reinterpret_cast<const float2 *>(base + s0);
+      r[0] = a.x; r[1 % VW] = a.y;
+    } else {
+      r[0] = base[s0];
+    }
+  }
+  __device__ __forceinline__ void store(float *base, const float (&r)[VW]) const {
+    if (VW == 8) {
+      if (va) *reinterpret_cast<float4 *>(base + s0) = make_float4(r[0], r[1], r[2], r[3]);
+      if (vb) *reinterpret_cast<float4 *>(base + s0 + 128) = make_float4(r[4 % VW], r[5 % VW], r[6 % VW], r[7 % VW]);
+    } else if (VW == 2) {
+      *reinterpret_cast<float2 *>(base + s0) = make_float2(r[0], r[1 % VW]);
+    } else {
+      base[s0] = r[0];
+    }
+  }
+  __device__ __forceinline__ int slice(int k) const { return VW == 8 ? s0 + (k < 4 ? k : 124 + k) : s0 + k; }
+  __device__ __forceinline__ bool valid(int k) const { return VW == 8 ? (k < 4 ? va : vb) : true; }
+};
+
+// Map a thread to (unit, slice set).  VW = 8: one warp per (unit, 256-slice block);
+// otherwise one thread per (unit, VW slices).  Returns false past the end.
+template <int VW>
+__device__ __forceinline__ bool map_thread(long long units, int S, long long &unit, Slices<VW> &sl) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (VW == 8) {
+    const int nblk = (S + 255) / 256;
+    const long long w = t >> 5;
+    if (w >= units * nblk) return false;
+    unit = w / nblk;
+    const int blk = (int)(w - unit * nblk);
+    sl.s0 = blk * 256 + (int)(threadIdx.x & 31) * 4;
+    sl.va = sl.s0 < S;
+    sl.vb = sl.s0 + 128 < S;
+  } else {
+    const int nsg = S / VW;
+    if (t >= units * nsg) return false;
+    unit = t / nsg;
+    sl.s0 = (int)(t - unit * nsg) * VW;
+    sl.va = sl.vb = true;
+  }
+  return true;
+}
+
+template <int VW>
+static inline long long threads_for(long long units, int S) {
+  return VW == 8 ? units * ((S + 255) / 256) * 32 : units * (S / VW);
 }
 
 // ===========================================================================
@@ -459,7 +515,7 @@ __device__ __forceinline__ void ray_rows(const float4 o, int i, int N, int &ylo,
 
 template <int VW>
 __device__ __forceinline__ void radon_ray(const float *__restrict__ img, size_t S, int N, const float4 o, int i,
-                                          float (&acc)[VW]) {
+                                          const Slices<VW> &sl, float (&acc)[VW]) {
   int ylo, yhi;
   ray_rows(o, i, N, ylo, yhi);
   const float fi = (float)i, fim = (float)(i - 1), fip = (float)(i + 1);
@@ -484,7 +540,7 @@ __device__ __forceinline__ void radon_ray(const float *__restrict__ img, size_t 
       const float wgt = 1.0f - fabsf(__fsub_rn(__fadd_rn(__fmul_rn((float)x, o.x), d), fi));
       if (wgt > 0.f) {
         float val[VW];
-        ldv<VW>(row + (size_t)x * S, val);
+        sl.load(row + (size_t)x * S, val);
 #pragma unroll
         for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(wgt, val[k]));
       }
@@ -492,29 +548,111 @@ __device__ __forceinline__ void radon_ray(const float *__restrict__ img, size_t 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Ray tables.  The geometry is fixed for a solve, so the (pixel, weight) list of
+// every ray -- the reference's own row bounds and hat weights, in its row-major
+// order -- is built once per problem (ray_count / ray_fill) and the iteration's
+// forward projection streams it (radon_table): same sums in the same order,
+// without the per-row bound computation.  Entry = (pixel index, weight).
+// ---------------------------------------------------------------------------
+template <bool FILL>
+__device__ __forceinline__ int ray_walk(const float4 o, int i, int N, int2 *out) {
+  int ylo, yhi;
+  ray_rows(o, i, N, ylo, yhi);
+  const float fi = (float)i, fim = (float)(i - 1), fip = (float)(i + 1);
+  int n = 0;
+  for (int y = ylo; y <= yhi; ++y) {
+    const float d = __fadd_rn(__fmul_rn((float)y, o.y), o.z);
+    int xl, xh;
+    if (o.x == 0.f) {
+      if (d > fim && d < fip) { xl = 0; xh = N - 1; } else continue;
+    } else if (o.x > 0.f) {
+      xl = __float2int_rz(__fmul_rn(__fsub_rn(fim, d), o.w));
+      xh = __float2int_rz(__fmul_rn(__fsub_rn(fip, d), o.w));
+    } else {
+      xl = __float2int_rz(__fmul_rn(__fsub_rn(fip, d), o.w));
+      xh = __float2int_rz(__fmul_rn(__fsub_rn(fim, d), o.w));
+    }
+    xl = max(xl, 0);
+    xh = min(xh, N - 1);
+    for (int x = xl; x <= xh; ++x) {
+      const float wgt = 1.0f - fabsf(__fsub_rn(__fadd_rn(__fmul_rn((float)x, o.x), d), fi));
+      if (wgt > 0.f) {
+        if (FILL) out[n] = make_int2(y * N + x, __float_as_int(wgt));
+        ++n;
+      }
+    }
+  }
+  return n;
+}
+
+__global__ void k_ray_count(const float4 *__restrict__ ofs, int N, int nd, int nang, int *__restrict__ count) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nd * nang) return;
+  const int j = t / nd, i = t - j * nd;
+  count[t] = ray_walk<false>(__ldg(ofs + j), i, N, nullptr);
+}
+
+__global__ void k_ray_fill(const float4 *__restrict__ ofs, int N, int nd, int nang, const long long *__restrict__ start,
+                           int2 *__restrict__ ent) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nd * nang) return;
+  const int j = t / nd, i = t - j * nd;
+  ray_walk<true>(__ldg(ofs + j), i, N, ent + start[t]);
+}
+
+template <int VW>
+__device__ __forceinline__ void radon_table(const float *__restrict__ img, size_t S, const int2 *__restrict__ ent,
+                                            int n, const Slices<VW> &sl, float (&acc)[VW]) {
+#pragma unroll
+  for (int k = 0; k < VW; ++k) acc[k] = 0.f;
+  int e = 0;
+  for (; e + 2 <= n; e += 2) {  // two entries in flight
+    const int2 a = __ldg(ent + e), b = __ldg(ent + e + 1);
+    float va[VW], vb[VW];
+    sl.load(img + (size_t)a.x * S, va);
+    sl.load(img + (size_t)b.x * S, vb);
+    const float wa = __int_as_float(a.y), wb = __int_as_float(b.y);
+#pragma unroll
+    for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(wa, va[k]));
+#pragma unroll
+    for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(wb, vb[k]));
+  }
+  if (e < n) {
+    const int2 a = __ldg(ent + e);
+    float va[VW];
+    sl.load(img + (size_t)a.x * S, va);
+    const float wa = __int_as_float(a.y);
+#pragma unroll
+    for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(wa, va[k]));
+  }
+}
+
 // k_fwd: radon of ubar fused with update_lambda_KL (3-D :690-704) or _L2 (:677-688).
-// thread = one (bin, slice group of VW).
 template <int DISC, int VW>
 __global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
   const Dims d = P.d;
-  const int nsg = d.S / VW;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)d.nd * d.nang * nsg) return;
-  const int b = (int)(t / nsg);
-  const int s0 = (int)(t - (long long)b * nsg) * VW;
+  long long unit;
+  Slices<VW> sl;
+  if (!map_thread<VW>((long long)d.nd * d.nang, d.S, unit, sl)) return;
+  const int b = (int)unit;
   const int j = b / d.nd, i = b - j * d.nd;
-  const float4 o = __ldg(P.ofs + j);
   float acc[VW];
-  radon_ray<VW>(P.ubar + s0, d.S, d.N, o, i, acc);
-  const size_t q = (size_t)b * d.S + s0;
-  stv<VW>(P.ku + q, acc);
+  if (P.ray_start) {
+    const long long r0 = __ldg(P.ray_start + b), r1 = __ldg(P.ray_start + b + 1);
+    radon_table<VW>(P.ubar, d.S, P.ray_ent + r0, (int)(r1 - r0), sl, acc);
+  } else {
+    radon_ray<VW>(P.ubar, d.S, d.N, __ldg(P.ofs + j), i, sl, acc);
+  }
+  const size_t q = (size_t)b * d.S;
+  sl.store(P.ku + q, acc);
   float lam[VW], f[VW];
-  ldw<VW>(P.lam + q, lam);
-  ldv<VW>(P.f + q, f);
+  sl.loadw(P.lam + q, lam);
+  sl.load(P.f + q, f);
   const float sd = P.sigma_data;
 #pragma unroll
   for (int k = 0; k < VW; ++k) {
-    const float m = __ldg(P.mu + (s0 + k) / d.Nz);
+    const float m = sl.valid(k) ? __ldg(P.mu + sl.slice(k) / d.Nz) : 0.f;
     if (DISC == KL) {
       const float sv = lam[k] + sd * acc[k];
       const float wv = sv - m;
@@ -524,7 +662,7 @@ __global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
       lam[k] = (lam[k] + sd * (acc[k] - f[k])) * m;
     }
   }
-  stv<VW>(P.lam + q, lam);
+  sl.store(P.lam + q, lam);
 }
 
 // ===========================================================================
@@ -533,7 +671,8 @@ __global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
 // ===========================================================================
 template <int VW>
 __device__ __forceinline__ void radon_ad_pixel(const float *__restrict__ lam, size_t S, int nd, int nang,
-                                               const float4 *__restrict__ ofs, float xf, float yf, float (&acc)[VW]) {
+                                               const float4 *__restrict__ ofs, float xf, float yf,
+                                               const Slices<VW> &sl, float (&acc)[VW]) {
 #pragma unroll
   for (int k = 0; k < VW; ++k) acc[k] = 0.f;
   const float fnd = (float)nd;
@@ -549,12 +688,12 @@ __device__ __forceinline__ void radon_ad_pixel(const float *__restrict__ lam, si
       const float *lj = lam + (size_t)j * nd * S;
       float a[VW], b[VW];
       if (il >= 0) {
-        ldv<VW>(lj + (size_t)il * S, a);
+        sl.load(lj + (size_t)il * S, a);
 #pragma unroll
         for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(q, a[k]));
       }
       if (il <= nd - 2) {
-        ldv<VW>(lj + (size_t)(il + 1) * S, b);
+        sl.load(lj + (size_t)(il + 1) * S, b);
 #pragma unroll
         for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(p, b[k]));
       }
@@ -562,57 +701,31 @@ __device__ __forceinline__ void radon_ad_pixel(const float *__restrict__ lam, si
   }
 }
 
-// k_primal: radon_ad of lambda + update_u (3-D :706-729, 2-D :340-357) +
-// update_p (3-D :734-757, 2-D :359-376) + extrapolation and swap (:1217-1221).
-// thread = one (pixel, slice group of VW).
+// update_u (3-D :706-729, 2-D :340-357) + update_p (3-D :734-757, 2-D :359-376) +
+// extrapolation and swap (:1217-1221) for UW consecutive slices from s0.
 template <int DIM, bool TGV, int UW>
-__device__ __forceinline__ void primal_update(const IterParams &P, int x, int y, int s0, const float (&kstar)[UW]);
-
-template <int DIM, bool TGV, int VW>
-__global__ void __launch_bounds__(256) k_primal(const IterParams P) {
-  const Dims d = P.d;
-  const int nsg = d.S / VW;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)d.N * d.N * nsg) return;
-  const int pix = (int)(t / nsg);
-  const int s0 = (int)(t - (long long)pix * nsg) * VW;
-  const int y = pix / d.N, x = pix - y * d.N;
-  float kstar[VW];
-  radon_ad_pixel<VW>(P.lam + s0, d.S, d.nd, d.nang, P.ofs, (float)x, (float)y, kstar);
-  // the memory-bound update part works on at most 4 slices at a time (registers)
-  constexpr int UW = VW > 4 ? 4 : VW;
-#pragma unroll
-  for (int h = 0; h < VW / UW; ++h) {
-    float ks[UW];
-#pragma unroll
-    for (int k = 0; k < UW; ++k) ks[k] = kstar[h * UW + k];
-    primal_update<DIM, TGV, UW>(P, x, y, s0 + h * UW, ks);
-  }
-}
-
-template <int DIM, bool TGV, int VW>
-__device__ __forceinline__ void primal_update(const IterParams &P, int x, int y, int s0, const float (&kstar)[VW]) {
+__device__ __forceinline__ void primal_update(const IterParams &P, int x, int y, int s0, const float (&kstar)[UW]) {
   const Dims d = P.d;
   const size_t S = d.S, rowS = (size_t)d.N * S, vol = d.vol, i = ((size_t)y * d.N + x) * S + s0;
-  int z[VW];
+  int z[UW];
 #pragma unroll
-  for (int k = 0; k < VW; ++k) z[k] = (DIM == 3) ? (s0 + k) % d.Nz : 0;
+  for (int k = 0; k < UW; ++k) z[k] = (DIM == 3) ? (s0 + k) % d.Nz : 0;
 
   // divergence of v: backward differences (adjoint of the forward gradient)
   const float *__restrict__ v = P.v;
-  float a[VW], b[VW], am[VW], bm[VW], uo[VW], un[VW], ub[VW];
-  ldw<VW>(v + i, a);
-  ldw<VW>(v + vol + i, b);
-  if (x > 0) ldw<VW>(v + i - S, am);
-  if (y > 0) ldw<VW>(v + vol + i - rowS, bm);
-  ldw<VW>(P.u + i, uo);
-  float c[VW], cprev = 0.f;
+  float a[UW], b[UW], am[UW], bm[UW], uo[UW], un[UW], ub[UW];
+  ldw<UW>(v + i, a);
+  ldw<UW>(v + vol + i, b);
+  if (x > 0) ldw<UW>(v + i - S, am);
+  if (y > 0) ldw<UW>(v + vol + i - rowS, bm);
+  ldw<UW>(P.u + i, uo);
+  float c[UW], cprev = 0.f;
   if (DIM == 3) {
-    ldw<VW>(v + 2 * vol + i, c);
+    ldw<UW>(v + 2 * vol + i, c);
     if (z[0] > 0) cprev = v[2 * vol + i - 1];
   }
 #pragma unroll
-  for (int k = 0; k < VW; ++k) {
+  for (int k = 0; k < UW; ++k) {
     float ak = a[k], bk = b[k];
     if (x == d.N - 1) ak = 0.f;
     if (x > 0) ak -= am[k];
@@ -632,8 +745,8 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
     un[k] = r;
     ub[k] = 2.0f * r - uo[k];
   }
-  stv<VW>(P.ubar + i, ub);
-  stv<VW>(P.u + i, un);
+  stv<UW>(P.ubar + i, ub);
+  stv<UW>(P.u + i, un);
 
   if (TGV) {
     const float *__restrict__ w = P.w;
@@ -642,20 +755,20 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
     const int rx[3] = {0, DIM == 3 ? 3 : 2, 4}, ry[3] = {DIM == 3 ? 3 : 2, 1, 5}, rz[3] = {4, 5, 2};
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      float wa[VW], wan[VW], wb[VW], wbn[VW], po[VW], vk[VW], pn[VW], pb[VW];
-      ldw<VW>(w + rx[k] * vol + i, wa);
-      ldw<VW>(w + ry[k] * vol + i, wb);
-      if (x < d.N - 1) ldw<VW>(w + rx[k] * vol + i + S, wan);
-      if (y < d.N - 1) ldw<VW>(w + ry[k] * vol + i + rowS, wbn);
-      ldw<VW>(P.p + k * vol + i, po);
-      ldw<VW>(v + k * vol + i, vk);
-      float wc[VW], wcnext = 0.f;
+      float wa[UW], wan[UW], wb[UW], wbn[UW], po[UW], vk[UW], pn[UW], pb[UW];
+      ldw<UW>(w + rx[k] * vol + i, wa);
+      ldw<UW>(w + ry[k] * vol + i, wb);
+      if (x < d.N - 1) ldw<UW>(w + rx[k] * vol + i + S, wan);
+      if (y < d.N - 1) ldw<UW>(w + ry[k] * vol + i + rowS, wbn);
+      ldw<UW>(P.p + k * vol + i, po);
+      ldw<UW>(v + k * vol + i, vk);
+      float wc[UW], wcnext = 0.f;
       if (DIM == 3) {
-        ldw<VW>(w + rz[k] * vol + i, wc);
-        if (z[VW - 1] < d.Nz - 1) wcnext = w[rz[k] * vol + i + VW];
+        ldw<UW>(w + rz[k] * vol + i, wc);
+        if (z[UW - 1] < d.Nz - 1) wcnext = w[rz[k] * vol + i + UW];
       }
 #pragma unroll
-      for (int e = 0; e < VW; ++e) {
+      for (int e = 0; e < UW; ++e) {
         float A = -wa[e], B = -wb[e];
         if (x == 0) A = 0.f;
         if (x < d.N - 1) A += wan[e];
@@ -665,7 +778,7 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
         if (DIM == 3) {
           float Cz = -wc[e];
           if (z[e] == 0) Cz = 0.f;
-          if (z[e] < d.Nz - 1) Cz += (e < VW - 1 ? wc[e + 1] : wcnext);
+          if (z[e] < d.Nz - 1) Cz += (e < UW - 1 ? wc[e + 1] : wcnext);
           Cz /= P.stepsize;
           r = po[e] + P.tau * (vk[e] + A + B + Cz);
         } else {
@@ -674,9 +787,31 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
         pn[e] = r;
         pb[e] = 2.0f * r - po[e];
       }
-      stv<VW>(P.pbar + k * vol + i, pb);
-      stv<VW>(P.p + k * vol + i, pn);
+      stv<UW>(P.pbar + k * vol + i, pb);
+      stv<UW>(P.p + k * vol + i, pn);
     }
+  }
+}
+
+// k_primal: radon_ad of lambda, then the primal update of each chunk of slices.
+template <int DIM, bool TGV, int VW>
+__global__ void __launch_bounds__(256) k_primal(const IterParams P) {
+  const Dims d = P.d;
+  long long unit;
+  Slices<VW> sl;
+  if (!map_thread<VW>((long long)d.N * d.N, d.S, unit, sl)) return;
+  const int pix = (int)unit;
+  const int y = pix / d.N, x = pix - y * d.N;
+  float kstar[VW];
+  radon_ad_pixel<VW>(P.lam, d.S, d.nd, d.nang, P.ofs, (float)x, (float)y, sl, kstar);
+  if (VW == 8) {
+    float ka[4], kb[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { ka[k] = kstar[k]; kb[k] = kstar[(4 + k) % VW]; }
+    if (sl.va) primal_update<DIM, TGV, 4>(P, x, y, sl.s0, ka);
+    if (sl.vb) primal_update<DIM, TGV, 4>(P, x, y, sl.s0 + 128, kb);
+  } else {
+    primal_update<DIM, TGV, VW>(P, x, y, sl.s0, kstar);
   }
 }
 
@@ -686,27 +821,25 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
 template <int VW>
 __global__ void k_radon(const float *__restrict__ img, float *__restrict__ sino, const float4 *__restrict__ ofs,
                         int N, int nd, int nang, int S) {
-  const int nsg = S / VW;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nd * nang * nsg) return;
-  const int b = (int)(t / nsg), s0 = (int)(t - (long long)b * nsg) * VW;
-  const int j = b / nd, i = b - j * nd;
+  long long unit;
+  Slices<VW> sl;
+  if (!map_thread<VW>((long long)nd * nang, S, unit, sl)) return;
+  const int b = (int)unit, j = b / nd, i = b - j * nd;
   float acc[VW];
-  radon_ray<VW>(img + s0, S, N, __ldg(ofs + j), i, acc);
-  stv<VW>(sino + (size_t)b * S + s0, acc);
+  radon_ray<VW>(img, S, N, __ldg(ofs + j), i, sl, acc);
+  sl.store(sino + (size_t)b * S, acc);
 }
 
 template <int VW>
 __global__ void k_radon_ad(const float *__restrict__ sino, float *__restrict__ img, const float4 *__restrict__ ofs,
                            int N, int nd, int nang, int S) {
-  const int nsg = S / VW;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)N * N * nsg) return;
-  const int pix = (int)(t / nsg), s0 = (int)(t - (long long)pix * nsg) * VW;
-  const int y = pix / N, x = pix - y * N;
+  long long unit;
+  Slices<VW> sl;
+  if (!map_thread<VW>((long long)N * N, S, unit, sl)) return;
+  const int pix = (int)unit, y = pix / N, x = pix - y * N;
   float acc[VW];
-  radon_ad_pixel<VW>(sino + s0, S, nd, nang, ofs, (float)x, (float)y, acc);
-  stv<VW>(img + (size_t)pix * S + s0, acc);
+  radon_ad_pixel<VW>(sino, S, nd, nang, ofs, (float)x, (float)y, sl, acc);
+  sl.store(img + (size_t)pix * S, acc);
 }
 
 // out[c][r] = in[r][c]: host layout [S][X] <-> device layout [X][S], 32x32 tiles,
@@ -843,12 +976,12 @@ cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st) 
   return tgv ? launch_dual_t<2, true>(P, cpl, st) : launch_dual_t<2, false>(P, cpl, st);
 }
 
-// slices per lane: 4 when S allows aligned float4 access, else 2, else 1
-static inline int vec_width(int S) { return (S % 8 == 0) ? 8 : (S % 4 == 0) ? 4 : (S % 2 == 0 ? 2 : 1); }
+// slices per lane: 8 (two float4 chunks) when S is a multiple of 4, else 2, else 1
+static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 : 1); }
 
 template <int VW>
 static void fwd_vw(const IterParams &P, int disc, cudaStream_t st) {
-  const unsigned g = blocks_for((long long)P.d.nd * P.d.nang * (P.d.S / VW), 256);
+  const unsigned g = blocks_for(threads_for<VW>((long long)P.d.nd * P.d.nang, P.d.S), 256);
   if (disc == KL) k_fwd<KL, VW><<<g, 256, 0, st>>>(P);
   else k_fwd<L2, VW><<<g, 256, 0, st>>>(P);
 }
@@ -856,7 +989,6 @@ static void fwd_vw(const IterParams &P, int disc, cudaStream_t st) {
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
   const int vw = vec_width(P.d.S);
   if (vw == 8) fwd_vw<8>(P, disc, st);
-  else if (vw == 4) fwd_vw<4>(P, disc, st);
   else if (vw == 2) fwd_vw<2>(P, disc, st);
   else fwd_vw<1>(P, disc, st);
   return cudaGetLastError();
@@ -864,7 +996,7 @@ cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
 
 template <int VW>
 static void primal_vw(const IterParams &P, int tgv, cudaStream_t st) {
-  const unsigned g = blocks_for((long long)P.d.N * P.d.N * (P.d.S / VW), 256);
+  const unsigned g = blocks_for(threads_for<VW>((long long)P.d.N * P.d.N, P.d.S), 256);
   if (P.d.dim == 3) {
     if (tgv) k_primal<3, true, VW><<<g, 256, 0, st>>>(P);
     else k_primal<3, false, VW><<<g, 256, 0, st>>>(P);
@@ -877,33 +1009,48 @@ static void primal_vw(const IterParams &P, int tgv, cudaStream_t st) {
 cudaError_t launch_primal(const IterParams &P, int tgv, cudaStream_t st) {
   const int vw = vec_width(P.d.S);
   if (vw == 8) primal_vw<8>(P, tgv, st);
-  else if (vw == 4) primal_vw<4>(P, tgv, st);
   else if (vw == 2) primal_vw<2>(P, tgv, st);
   else primal_vw<1>(P, tgv, st);
   return cudaGetLastError();
 }
 
-static inline bool aligned(const void *p, int vw) { return ((uintptr_t)p % (4 * vw)) == 0; }
+static inline bool aligned(const void *p, int bytes) { return ((uintptr_t)p % bytes) == 0; }
+
+static int proj_width(const void *a, const void *b, int S) {
+  int vw = vec_width(S);
+  if (vw == 8 && !(aligned(a, 16) && aligned(b, 16))) vw = (S % 2 == 0) ? 2 : 1;
+  if (vw == 2 && !(aligned(a, 8) && aligned(b, 8))) vw = 1;
+  return vw;
+}
 
 cudaError_t launch_radon(const float *img, float *sino, const float4 *ofs, int N, int nd, int nang, int S,
                          cudaStream_t st) {
-  int vw = vec_width(S);
-  while (vw > 1 && !(aligned(img, vw > 4 ? 4 : vw) && aligned(sino, vw > 4 ? 4 : vw))) vw /= 2;
-  if (vw == 8) k_radon<8><<<blocks_for((long long)nd * nang * (S / 8), 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
-  else if (vw == 4) k_radon<4><<<blocks_for((long long)nd * nang * (S / 4), 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
-  else if (vw == 2) k_radon<2><<<blocks_for((long long)nd * nang * (S / 2), 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
-  else k_radon<1><<<blocks_for((long long)nd * nang * S, 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
+  const long long units = (long long)nd * nang;
+  const int vw = proj_width(img, sino, S);
+  if (vw == 8) k_radon<8><<<blocks_for(threads_for<8>(units, S), 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
+  else if (vw == 2) k_radon<2><<<blocks_for(threads_for<2>(units, S), 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
+  else k_radon<1><<<blocks_for(threads_for<1>(units, S), 256), 256, 0, st>>>(img, sino, ofs, N, nd, nang, S);
   return cudaGetLastError();
 }
 
 cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, int N, int nd, int nang, int S,
                             cudaStream_t st) {
-  int vw = vec_width(S);
-  while (vw > 1 && !(aligned(img, vw > 4 ? 4 : vw) && aligned(sino, vw > 4 ? 4 : vw))) vw /= 2;
-  if (vw == 8) k_radon_ad<8><<<blocks_for((long long)N * N * (S / 8), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
-  else if (vw == 4) k_radon_ad<4><<<blocks_for((long long)N * N * (S / 4), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
-  else if (vw == 2) k_radon_ad<2><<<blocks_for((long long)N * N * (S / 2), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
-  else k_radon_ad<1><<<blocks_for((long long)N * N * S, 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
+  const long long units = (long long)N * N;
+  const int vw = proj_width(img, sino, S);
+  if (vw == 8) k_radon_ad<8><<<blocks_for(threads_for<8>(units, S), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
+  else if (vw == 2) k_radon_ad<2><<<blocks_for(threads_for<2>(units, S), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
+  else k_radon_ad<1><<<blocks_for(threads_for<1>(units, S), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ray_count(const float4 *ofs, int N, int nd, int nang, int *count, cudaStream_t st) {
+  k_ray_count<<<blocks_for((long long)nd * nang, 128), 128, 0, st>>>(ofs, N, nd, nang, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ray_fill(const float4 *ofs, int N, int nd, int nang, const long long *start, int2 *ent,
+                            cudaStream_t st) {
+  k_ray_fill<<<blocks_for((long long)nd * nang, 128), 128, 0, st>>>(ofs, N, nd, nang, start, ent);
   return cudaGetLastError();
 }
 
