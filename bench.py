@@ -51,12 +51,14 @@ def peaks():
 def algorithmic_bytes(V, Sb):
     """Bytes one iteration must move (3-D TGV): 172 per voxel-channel + 16 per bin.
 
-    k_dual   reads ubar 4, pbar 12, v 12, w 24; writes v 12, w 24        (88 B/voxel-ch)
-    k_fwd    reads f 4, lambda 4; writes lambda 4, K ubar 4              (16 B/bin; + ubar 4 B/voxel-ch re-read)
-    k_primal reads u 4, p 12, v 12, w 24, lambda 4/bin; writes u, ubar 4+4, p, pbar 12+12 (84 B/voxel-ch)
+    Per kernel (what each launch must read and write at least once):
+    k_dual   reads ubar 4, pbar 12, v 12, w 24; writes v 12, w 24          (88 B/voxel-ch)
+    k_fwd    reads ubar 4 B/voxel-ch, f 4, lambda 4; writes lambda 4, K ubar 4 (16 B/bin)
+    k_bp     reads lambda 4 B/bin; writes K* lambda 4 B/voxel-ch
+    k_update reads u 4, p 12, v 12, w 24, K* lambda 4; writes u 4, ubar 4, p 12, pbar 12 (88 B/voxel-ch)
     """
     return {"iteration": 172 * V + 16 * Sb, "k_dual": 88 * V, "k_fwd": 4 * V + 16 * Sb,
-            "k_primal": 84 * V + 4 * Sb}
+            "k_bp": 4 * V + 4 * Sb, "k_update": 88 * V}
 
 
 def make_problem_data(seed=0):
@@ -276,6 +278,7 @@ def run_ours(args, rank, world, local):
     solver_gbs = alg["iteration"] / (it_ms / 1e3) / 1e9
     launches = prob.launches_per_iteration * args.steps
     ne = prob.scalars["normest"]
+    tuning = prob.tuning
     prob.close()
 
     # ---- end to end through the reference-facing entry point, host buffers
@@ -302,7 +305,7 @@ def run_ours(args, rank, world, local):
                       "regularisation": "TGV", "stated_iterations": W["stated_iterations"],
                       "time_for_stated_iterations_s": it_ms * W["stated_iterations"] / 1e3,
                       "l2": "inputs larger than L2 (solver state 1.1 GB per replica)",
-                      "parallelism": f"replicas x{world}", "normest": ne},
+                      "parallelism": f"replicas x{world}", "normest": ne, "autotuned": tuning},
            "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                         "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
                         "algorithmic_bytes_per_launch": alg[top], "ms_per_launch": kms[top]},

@@ -42,7 +42,7 @@ class GtDesc(ctypes.Structure):
         ("stepsize", ctypes.c_float), ("alpha0", ctypes.c_double), ("alpha1", ctypes.c_double),
         ("mu", ctypes.POINTER(ctypes.c_double)), ("discrepancy", ctypes.c_int), ("regularisation", ctypes.c_int),
         ("coupling", ctypes.c_int), ("normest", ctypes.c_double), ("device", ctypes.c_int),
-        ("stream", ctypes.c_void_p),
+        ("stream", ctypes.c_void_p), ("autotune", ctypes.c_int),
     ]
 
 
@@ -56,6 +56,7 @@ _SIGS = {
     "gt_get_state": (ctypes.c_int, [_P, ctypes.c_int, _P]),
     "gt_set_state": (ctypes.c_int, [_P, ctypes.c_int, _P]),
     "gt_get_scalars": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "gt_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     "gt_gap": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
     "gt_radon": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "gt_radon_ad": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),

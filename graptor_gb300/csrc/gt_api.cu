@@ -5,7 +5,12 @@
 
 #include <cmath>
 #include <cstdarg>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstdio>
+#include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -17,7 +22,8 @@
 namespace gt {
 cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st);
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st);
-cudaError_t launch_primal(const IterParams &P, int tgv, cudaStream_t st);
+cudaError_t launch_bp(const IterParams &P, cudaStream_t st);
+cudaError_t launch_update(const IterParams &P, int tgv, cudaStream_t st);
 cudaError_t launch_radon(const float *img, float *sino, const float4 *ofs, int N, int nd, int nang, int S,
                          cudaStream_t st);
 cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, int N, int nd, int nang, int S,
@@ -31,6 +37,8 @@ cudaError_t fill_f32(float *x, size_t n, float v, cudaStream_t st);
 cudaError_t launch_ray_count(const float4 *ofs, int N, int nd, int nang, int *count, cudaStream_t st);
 cudaError_t launch_ray_fill(const float4 *ofs, int N, int nd, int nang, const long long *start, int2 *ent,
                             cudaStream_t st);
+cudaError_t launch_bp_table(const float4 *ofs, int N, int nd, int nang, int2 *tab, cudaStream_t st);
+int num_proj_configs(int S, int which);
 }  // namespace gt
 
 namespace {
@@ -101,10 +109,11 @@ struct gt_problem {
   dvec4 *ofs64 = nullptr;
   float *mu_eff = nullptr;
   float *u = nullptr, *ubar = nullptr, *p = nullptr, *pbar = nullptr, *v = nullptr, *w = nullptr;
-  float *lam = nullptr, *f = nullptr, *ku = nullptr, *stage = nullptr;
+  float *lam = nullptr, *f = nullptr, *ku = nullptr, *stage = nullptr, *kstar = nullptr;
   void *rays = nullptr;        // ray table (offsets + entries), built at creation
   size_t ray_bytes = 0;
   gt::IterParams P{};
+  bool autotune = true;
   cudaGraphExec_t g_one = nullptr, g_chunk = nullptr;
   int chunk = 16;
   long long iters = 0;
@@ -113,17 +122,19 @@ struct gt_problem {
 
 namespace {
 
-// One iteration.  k_dual (memory-bound) and k_fwd (issue-bound) touch disjoint
-// outputs and only read what the previous k_primal wrote, so they run on two
-// streams and overlap; k_primal waits for both (a fork/join in the graph).
+// One iteration as a fork/join.  The projector chain k_fwd -> k_bp (issue- and
+// cache-bound) needs only ubar and lambda; k_dual (DRAM-bound) needs ubar, pbar,
+// v, w; they write disjoint fields, so they run on two streams and overlap.
+// k_update waits for both.
 int enqueue_iteration(gt_problem *p) {
   CK(cudaEventRecord(p->ev_fork, p->stream));
   CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
   CK(gt::launch_fwd(p->P, p->disc, p->side));
+  CK(gt::launch_bp(p->P, p->side));
   CK(gt::launch_dual(p->P, p->reg == GT_TGV, p->cpl, p->stream));
   CK(cudaEventRecord(p->ev_join, p->side));
   CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
-  CK(gt::launch_primal(p->P, p->reg == GT_TGV, p->stream));
+  CK(gt::launch_update(p->P, p->reg == GT_TGV, p->stream));
   return GT_OK;
 }
 
@@ -179,6 +190,77 @@ void set_scalars(gt_problem *p) {
   p->P.stepsize = p->stepsize;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner: times every launch shape of k_fwd and k_bp (gt_kernels.cu,
+// launch_fwd / launch_bp) with CUDA events on the problem's own buffers and keeps
+// the fastest; choices are cached per problem shape for the process lifetime.
+// It runs inside gt_set_data before the iterates are reset, so the extra
+// launches never touch the solve.
+using TuneKey = std::tuple<int, int, int, int, int, int, int>;
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune;
+
+int autotune(gt_problem *p) {
+  const int ncf = gt::num_proj_configs(p->d.S, 0), ncb = gt::num_proj_configs(p->d.S, 1);
+  p->P.fwd_cfg = 0;
+  p->P.bp_cfg = 0;
+  if ((ncf <= 1 && ncb <= 1) || !p->autotune) return GT_OK;
+  const TuneKey key{p->d.dim, p->d.N, p->d.S, p->d.nd, p->d.nang, p->disc, p->d.C};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      p->P.fwd_cfg = it->second.first;
+      p->P.bp_cfg = it->second.second;
+      return GT_OK;
+    }
+  }
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  // configurations interleaved over several rounds; each keeps its fastest round
+  float ms_cfg[2][8];
+  for (auto &r : ms_cfg) for (float &v : r) v = 1e30f;
+  int rc = GT_OK;
+  const bool log = std::getenv("GRAPTOR_TUNE_LOG") != nullptr;
+  for (int round = 0; round < 4 && rc == GT_OK; ++round) {
+    for (int which = 0; which < 2 && rc == GT_OK; ++which) {
+      const int nc = which == 0 ? ncf : ncb;
+      for (int c = 0; c < nc && rc == GT_OK; ++c) {
+        gt::IterParams Q = p->P;
+        if (which == 0) Q.fwd_cfg = c; else Q.bp_cfg = c;
+        auto launch = [&]() { return which == 0 ? gt::launch_fwd(Q, p->disc, p->stream) : gt::launch_bp(Q, p->stream); };
+        cudaError_t e = launch();  // warm-up
+        if (e == cudaSuccess) e = cudaEventRecord(e0, p->stream);
+        for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = launch();
+        if (e == cudaSuccess) e = cudaEventRecord(e1, p->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) { rc = cuda_err(e, "autotune", __LINE__); break; }
+        ms_cfg[which][c] = std::min(ms_cfg[which][c], ms / 2);
+      }
+    }
+  }
+  int best[2] = {0, 0};
+  for (int which = 0; which < 2; ++which)
+    for (int c = 1; c < (which == 0 ? ncf : ncb); ++c)
+      if (ms_cfg[which][c] < ms_cfg[which][best[which]]) best[which] = c;
+  if (log && rc == GT_OK)
+    for (int which = 0; which < 2; ++which)
+      for (int c = 0; c < (which == 0 ? ncf : ncb); ++c)
+        fprintf(stderr, "graptor autotune %s cfg %d: %.4f ms%s\n", which ? "k_bp" : "k_fwd", c, ms_cfg[which][c],
+                c == best[which] ? " *" : "");
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  p->P.fwd_cfg = best[0];
+  p->P.bp_cfg = best[1];
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = {best[0], best[1]};
+  return GT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -188,7 +270,7 @@ const char *gt_version(void) { return "graptor_gb300 0.1 (sm_103a)"; }
 
 int gt_launches_per_iteration(const gt_problem *p) {
   if (!p) return 0;
-  return 2 + (p->d.C > 8 ? (p->d.C + 7) / 8 : 1);
+  return 3 + (p->d.C > 8 ? (p->d.C + 7) / 8 : 1);
 }
 
 int gt_problem_create(const gt_desc *desc, gt_problem **out) {
@@ -221,6 +303,7 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
   p->K = D.dim; p->KW = D.dim == 3 ? 6 : 3;
   p->stepsize = D.stepsize;
   p->alpha0 = D.alpha0; p->alpha1 = D.alpha1; p->ne_in = D.normest;
+  p->autotune = D.autotune != 0;
   p->mu.assign(D.mu, D.mu + D.C);
   angle_table(D.angles, D.N, D.nd, D.nang, p->ofs64h);
 
@@ -249,7 +332,8 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
       align256(fv * p->K),                                          // v
       tgv ? align256(fv * p->KW) : 0,                               // w
       align256(fb), align256(fb), align256(fb),                     // lam, f, ku
-      align256(std::max(fv, fb))};                                  // stage
+      align256(std::max(fv, fb)),                                   // stage
+      align256(fv)};                                                // kstar
   const int nsz = (int)(sizeof(sizes) / sizeof(sizes[0]));
   for (int k = 0; k < nsz; ++k) { off[k] = total; total += sizes[k]; }
   cudaError_t e = cudaMalloc(&p->block, total);
@@ -272,6 +356,7 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
   p->f = (float *)(b + off[10]);
   p->ku = (float *)(b + off[11]);
   p->stage = (float *)(b + off[12]);
+  p->kstar = (float *)(b + off[13]);
 
   std::vector<float> t32((size_t)D.nang * 4);
   for (size_t k = 0; k < t32.size(); ++k) t32[k] = (float)p->ofs64h[k];
@@ -296,7 +381,8 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
       return fail(cuda_err(e, "ray table count", __LINE__));
     for (int r = 0; r < nr; ++r) start[r + 1] = start[r] + cnt[r];
     const size_t off_b = align256(sizeof(long long) * (nr + 1));
-    p->ray_bytes = off_b + sizeof(int2) * (size_t)start[nr];
+    const size_t off_bp = off_b + align256(sizeof(int2) * (size_t)start[nr]);
+    p->ray_bytes = off_bp + sizeof(int2) * (size_t)D.N * D.N * D.nang;
     if ((e = cudaMalloc(&p->rays, p->ray_bytes)) != cudaSuccess) {
       cudaGetLastError();
       gt_problem_destroy(p);
@@ -307,17 +393,20 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
     if ((e = cudaMemcpyAsync(d_start, start.data(), sizeof(long long) * (nr + 1), cudaMemcpyHostToDevice,
                              p->stream)) != cudaSuccess ||
         (e = gt::launch_ray_fill(p->ofs, D.N, D.nd, D.nang, d_start, d_ent, p->stream)) != cudaSuccess ||
+        (e = gt::launch_bp_table(p->ofs, D.N, D.nd, D.nang, (int2 *)((char *)p->rays + off_bp), p->stream)) !=
+            cudaSuccess ||
         (e = cudaStreamSynchronize(p->stream)) != cudaSuccess)
       return fail(cuda_err(e, "ray table fill", __LINE__));
     p->P.ray_start = d_start;
     p->P.ray_ent = d_ent;
+    p->P.bp_tab = (const int2 *)((char *)p->rays + off_bp);
   }
 
   gt::IterParams &P = p->P;
   P.d = p->d;
   P.ofs = p->ofs; P.mu = p->mu_eff;
   P.u = p->u; P.ubar = p->ubar; P.p = p->p; P.pbar = p->pbar; P.v = p->v; P.w = p->w;
-  P.lam = p->lam; P.f = p->f; P.ku = p->ku;
+  P.lam = p->lam; P.f = p->f; P.ku = p->ku; P.kstar = p->kstar;
   *out = p;
   return GT_OK;
 }
@@ -376,6 +465,11 @@ int gt_set_data(gt_problem *p, const float *f_host, int make_feasible) {
   for (int c = 0; c < d.C; ++c)
     me[c] = (float)(p->disc == GT_KL ? p->mu[c] : p->mu[c] / (p->sigma + p->mu[c]));
   CK(cudaMemcpyAsync(p->mu_eff, me.data(), sizeof(float) * d.C, cudaMemcpyHostToDevice, p->stream));
+  // pick the projector launch shapes (uses lambda / ku / kstar as scratch: they are reset below)
+  {
+    const int rc = autotune(p);
+    if (rc) return rc;
+  }
   // zero iterates (tgv_radon :1160-1176)
   const size_t fv = sizeof(float) * d.vol;
   CK(cudaMemsetAsync(p->u, 0, fv, p->stream));
@@ -450,6 +544,13 @@ int gt_set_state(gt_problem *p, int field, const float *host) {
   return GT_OK;
 }
 
+int gt_get_tuning(gt_problem *p, int out[2]) {
+  if (!p || !out) return set_err(GT_ERR_ARG, "null argument");
+  out[0] = p->P.fwd_cfg;
+  out[1] = p->P.bp_cfg;
+  return GT_OK;
+}
+
 int gt_get_scalars(gt_problem *p, double out[4]) {
   if (!p || !out) return set_err(GT_ERR_ARG, "null argument");
   out[0] = p->ne; out[1] = p->sigma; out[2] = p->tau; out[3] = (double)p->iters;
@@ -462,24 +563,27 @@ int gt_gap(gt_problem *p, double out[4]) {
 }
 
 int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n) {
-  if (!p || !ms_out || reps < 1 || n < 3) return set_err(GT_ERR_ARG, "bad argument");
+  if (!p || !ms_out || reps < 1 || n < 4) return set_err(GT_ERR_ARG, "bad argument");
   if (!p->has_data) return set_err(GT_ERR_STATE, "gt_time_kernels before gt_set_data");
   CK(cudaSetDevice(p->device));
-  cudaEvent_t ev[4];
+  cudaEvent_t ev[5];
   for (auto &e : ev) CK(cudaEventCreate(&e));
-  float acc[3] = {0, 0, 0};
+  float acc[4] = {0, 0, 0, 0};
   int rc = GT_OK;
+  const bool tgv = p->reg == GT_TGV;
   for (int r = 0; r < reps && rc == GT_OK; ++r) {
-    cudaError_t e;
-    if ((e = cudaEventRecord(ev[0], p->stream)) != cudaSuccess) { rc = cuda_err(e, "event", __LINE__); break; }
-    if ((e = gt::launch_dual(p->P, p->reg == GT_TGV, p->cpl, p->stream)) != cudaSuccess) { rc = cuda_err(e, "k_dual", __LINE__); break; }
-    cudaEventRecord(ev[1], p->stream);
-    if ((e = gt::launch_fwd(p->P, p->disc, p->stream)) != cudaSuccess) { rc = cuda_err(e, "k_fwd", __LINE__); break; }
-    cudaEventRecord(ev[2], p->stream);
-    if ((e = gt::launch_primal(p->P, p->reg == GT_TGV, p->stream)) != cudaSuccess) { rc = cuda_err(e, "k_primal", __LINE__); break; }
-    cudaEventRecord(ev[3], p->stream);
-    if ((e = cudaEventSynchronize(ev[3])) != cudaSuccess) { rc = cuda_err(e, "event sync", __LINE__); break; }
-    for (int k = 0; k < 3; ++k) {
+    cudaError_t e = cudaEventRecord(ev[0], p->stream);
+    if (e == cudaSuccess) e = gt::launch_dual(p->P, tgv, p->cpl, p->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], p->stream);
+    if (e == cudaSuccess) e = gt::launch_fwd(p->P, p->disc, p->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2], p->stream);
+    if (e == cudaSuccess) e = gt::launch_bp(p->P, p->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[3], p->stream);
+    if (e == cudaSuccess) e = gt::launch_update(p->P, tgv, p->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[4], p->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
+    if (e != cudaSuccess) { rc = cuda_err(e, "kernel timing", __LINE__); break; }
+    for (int k = 0; k < 4; ++k) {
       float ms = 0;
       cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
       acc[k] += ms;
@@ -488,7 +592,7 @@ int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n) {
   }
   for (auto &e : ev) cudaEventDestroy(e);
   if (rc) return rc;
-  for (int k = 0; k < 3; ++k) ms_out[k] = acc[k] / reps;
+  for (int k = 0; k < 4; ++k) ms_out[k] = acc[k] / reps;
   return GT_OK;
 }
 

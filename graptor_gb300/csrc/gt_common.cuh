@@ -41,14 +41,17 @@ struct IterParams {
   float ainv0, ainv1;    // 1 / (alpha / normest^2)
   float stepsize;
   int cbase;             // first channel handled by a k_dual launch (0 unless C > 8)
+  int fwd_cfg, bp_cfg;   // projector launch shapes (see launch_fwd / launch_bp)
   const float4 *ofs;     // [nang] (X, Y, offset, Xinv)
   const long long *ray_start;  // [nd*nang + 1] ray table offsets (null: walk rays on the fly)
   const int2 *ray_ent;         // (pixel, weight bits) entries of all rays
+  const int2 *bp_tab;          // [N*N][nang] (floor bin, fraction bits) of the back projection (or null)
   const float *mu;       // [C] mu (KL) or mu/(sigma+mu) (L2)
   float *u, *ubar;       // [vol]
   float *p, *pbar, *v;   // [K][vol]
   float *w;              // [KW][vol]
   float *lam, *f, *ku;   // [nbin]
+  float *kstar;          // [vol] back projection K* lambda
 };
 
 }  // namespace gt

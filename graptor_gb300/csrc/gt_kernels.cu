@@ -2,18 +2,20 @@
 //
 // One iteration of the reference loop (radon_tgv_primal_dual_3d.py:1194-1221:
 // update_v, update_w, NormV, NormW, radon, update_lambda, radon_ad, update_u,
-// update_p, two extrapolations) runs here as three kernels:
+// update_p, two extrapolations) runs here as four kernels:
 //
 //   k_dual    update_v + update_w + the coupled ball projections of v and w
 //             (one pass over ubar, pbar, v, w; writes v, w)
 //   k_fwd     forward projection `radon` of ubar fused with the data-term prox
 //             update_lambda (reads ubar, f, lambda; writes lambda and K ubar)
-//   k_primal  back projection `radon_ad` of lambda fused with update_u, update_p
-//             and both extrapolations (reads u, p, v, w, lambda; writes u, ubar, p, pbar)
+//   k_bp      back projection `radon_ad` of lambda (writes K* lambda)
+//   k_update  update_u, update_p and both extrapolations (reads u, p, v, w,
+//             K* lambda; writes u, ubar, p, pbar)
 //
-// k_dual and k_fwd only read what the previous k_primal wrote and write disjoint
-// fields, so they need no ordering between them.
+// k_dual and the chain k_fwd -> k_bp read only what the previous k_update wrote
+// and write disjoint fields, so they run concurrently.
 #include <cuda_runtime.h>
+#include <climits>
 #include <math.h>
 
 #include "gt_common.cuh"
@@ -409,6 +411,8 @@ template <int VW> __device__ __forceinline__ void stv(float *p, const float (&r)
 //   VW = 8: two float4 chunks, slices 4l..4l+3 and 128+4l..128+4l+3 of the warp's
 //           256-slice block (l = lane), so each load instruction of the warp
 //           reads 512 contiguous bytes; a warp never straddles pixels or bins.
+//   VW = 4: one float4 chunk, slices 4l..4l+3 of the warp's 128-slice block
+//           (twice the warps of VW = 8, half the registers).
 //   VW = 2, 1: VW consecutive slices per thread (S not a multiple of 4).
 // ===========================================================================
 template <int VW>
@@ -420,8 +424,12 @@ struct Slices {
       float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
       if (va) a = __ldg(reinterpret_cast<const float4 *>(base + s0));
       if (vb) b = __ldg(reinterpret_cast<const float4 *>(base + s0 + 128));
-      r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+      r[0] = a.x; r[1 % VW] = a.y; r[2 % VW] = a.z; r[3 % VW] = a.w;
       r[4 % VW] = b.x; r[5 % VW] = b.y; r[6 % VW] = b.z; r[7 % VW] = b.w;
+    } else if (VW == 4) {
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (va) a = __ldg(reinterpret_cast<const float4 *>(base + s0));
+      r[0] = a.x; r[1 % VW] = a.y; r[2 % VW] = a.z; r[3 % VW] = a.w;
     } else if (VW == 2) {
       const float2 a = __ldg(reinterpret_cast<const float2 *>(base + s0));
       r[0] = a.x; r[1 % VW] = a.y;
@@ -435,8 +443,12 @@ struct Slices {
       float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
       if (va) a = *reinterpret_cast<const float4 *>(base + s0);
       if (vb) b = *reinterpret_cast<const float4 *>(base + s0 + 128);
-      r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+      r[0] = a.x; r[1 % VW] = a.y; r[2 % VW] = a.z; r[3 % VW] = a.w;
       r[4 % VW] = b.x; r[5 % VW] = b.y; r[6 % VW] = b.z; r[7 % VW] = b.w;
+    } else if (VW == 4) {
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (va) a = *reinterpret_cast<const float4 *>(base + s0);
+      r[0] = a.x; r[1 % VW] = a.y; r[2 % VW] = a.z; r[3 % VW] = a.w;
     } else if (VW == 2) {
       const float2 a = *reinterpret_cast<const float2 *>(base + s0);
       r[0] = a.x; r[1 % VW] = a.y;
@@ -446,8 +458,10 @@ struct Slices {
   }
   __device__ __forceinline__ void store(float *base, const float (&r)[VW]) const {
     if (VW == 8) {
-      if (va) *reinterpret_cast<float4 *>(base + s0) = make_float4(r[0], r[1], r[2], r[3]);
+      if (va) *reinterpret_cast<float4 *>(base + s0) = make_float4(r[0], r[1 % VW], r[2 % VW], r[3 % VW]);
       if (vb) *reinterpret_cast<float4 *>(base + s0 + 128) = make_float4(r[4 % VW], r[5 % VW], r[6 % VW], r[7 % VW]);
+    } else if (VW == 4) {
+      if (va) *reinterpret_cast<float4 *>(base + s0) = make_float4(r[0], r[1 % VW], r[2 % VW], r[3 % VW]);
     } else if (VW == 2) {
       *reinterpret_cast<float2 *>(base + s0) = make_float2(r[0], r[1 % VW]);
     } else {
@@ -455,7 +469,7 @@ struct Slices {
     }
   }
   __device__ __forceinline__ int slice(int k) const { return VW == 8 ? s0 + (k < 4 ? k : 124 + k) : s0 + k; }
-  __device__ __forceinline__ bool valid(int k) const { return VW == 8 ? (k < 4 ? va : vb) : true; }
+  __device__ __forceinline__ bool valid(int k) const { return VW == 8 ? (k < 4 ? va : vb) : (VW == 4 ? va : true); }
 };
 
 // Map a thread to (unit, slice set).  VW = 8: one warp per (unit, 256-slice block);
@@ -463,15 +477,16 @@ struct Slices {
 template <int VW>
 __device__ __forceinline__ bool map_thread(long long units, int S, long long &unit, Slices<VW> &sl) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (VW == 8) {
-    const int nblk = (S + 255) / 256;
+  if (VW == 8 || VW == 4) {
+    const int span = VW * 32;
+    const int nblk = (S + span - 1) / span;
     const long long w = t >> 5;
     if (w >= units * nblk) return false;
     unit = w / nblk;
     const int blk = (int)(w - unit * nblk);
-    sl.s0 = blk * 256 + (int)(threadIdx.x & 31) * 4;
+    sl.s0 = blk * span + (int)(threadIdx.x & 31) * 4;
     sl.va = sl.s0 < S;
-    sl.vb = sl.s0 + 128 < S;
+    sl.vb = VW == 8 && sl.s0 + 128 < S;
   } else {
     const int nsg = S / VW;
     if (t >= units * nsg) return false;
@@ -484,7 +499,7 @@ __device__ __forceinline__ bool map_thread(long long units, int S, long long &un
 
 template <int VW>
 static inline long long threads_for(long long units, int S) {
-  return VW == 8 ? units * ((S + 255) / 256) * 32 : units * (S / VW);
+  return (VW == 8 || VW == 4) ? units * ((S + VW * 32 - 1) / (VW * 32)) * 32 : units * (S / VW);
 }
 
 // ===========================================================================
@@ -601,35 +616,55 @@ __global__ void k_ray_fill(const float4 *__restrict__ ofs, int N, int nd, int na
   ray_walk<true>(__ldg(ofs + j), i, N, ent + start[t]);
 }
 
-template <int VW>
+// acc += w * v per slice: the reference's separately rounded product and sum
+// (EXACT), or one fused multiply-add (the solver's hot loops)
+template <bool EXACT>
+__device__ __forceinline__ float mac(float acc, float w, float v) {
+  return EXACT ? __fadd_rn(acc, __fmul_rn(w, v)) : __fmaf_rn(w, v, acc);
+}
+
+template <int VW, bool EXACT, int UNR>
 __device__ __forceinline__ void radon_table(const float *__restrict__ img, size_t S, const int2 *__restrict__ ent,
                                             int n, const Slices<VW> &sl, float (&acc)[VW]) {
 #pragma unroll
   for (int k = 0; k < VW; ++k) acc[k] = 0.f;
+  // groups of UNR entries; the next group's entries are fetched while the current
+  // group's pixel loads are in flight (the entry -> pixel dependency is hidden)
+  int2 nx[UNR];
+#pragma unroll
+  for (int u = 0; u < UNR; ++u) nx[u] = u < n ? __ldg(ent + u) : make_int2(0, 0);
   int e = 0;
-  for (; e + 2 <= n; e += 2) {  // two entries in flight
-    const int2 a = __ldg(ent + e), b = __ldg(ent + e + 1);
-    float va[VW], vb[VW];
-    sl.load(img + (size_t)a.x * S, va);
-    sl.load(img + (size_t)b.x * S, vb);
-    const float wa = __int_as_float(a.y), wb = __int_as_float(b.y);
+  for (; e + UNR <= n; e += UNR) {
+    int2 en[UNR];
 #pragma unroll
-    for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(wa, va[k]));
+    for (int u = 0; u < UNR; ++u) en[u] = nx[u];
+    float v[UNR][VW];
 #pragma unroll
-    for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(wb, vb[k]));
+    for (int u = 0; u < UNR; ++u) sl.load(img + (size_t)en[u].x * S, v[u]);
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) nx[u] = (e + UNR + u < n) ? __ldg(ent + e + UNR + u) : make_int2(0, 0);
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const float w = __int_as_float(en[u].y);
+#pragma unroll
+      for (int k = 0; k < VW; ++k) acc[k] = mac<EXACT>(acc[k], w, v[u][k]);
+    }
   }
-  if (e < n) {
-    const int2 a = __ldg(ent + e);
-    float va[VW];
-    sl.load(img + (size_t)a.x * S, va);
-    const float wa = __int_as_float(a.y);
+  // remainder: its entries are already in nx
 #pragma unroll
-    for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(wa, va[k]));
+  for (int u = 0; u < UNR - 1; ++u) {
+    if (e + u < n) {
+      float va[VW];
+      sl.load(img + (size_t)nx[u].x * S, va);
+      const float wa = __int_as_float(nx[u].y);
+#pragma unroll
+      for (int k = 0; k < VW; ++k) acc[k] = mac<EXACT>(acc[k], wa, va[k]);
+    }
   }
 }
 
 // k_fwd: radon of ubar fused with update_lambda_KL (3-D :690-704) or _L2 (:677-688).
-template <int DISC, int VW>
+template <int DISC, int VW, int UNR>
 __global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
   const Dims d = P.d;
   long long unit;
@@ -640,7 +675,7 @@ __global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
   float acc[VW];
   if (P.ray_start) {
     const long long r0 = __ldg(P.ray_start + b), r1 = __ldg(P.ray_start + b + 1);
-    radon_table<VW>(P.ubar, d.S, P.ray_ent + r0, (int)(r1 - r0), sl, acc);
+    radon_table<VW, false, UNR>(P.ubar, d.S, P.ray_ent + r0, (int)(r1 - r0), sl, acc);
   } else {
     radon_ray<VW>(P.ubar, d.S, d.N, __ldg(P.ofs + j), i, sl, acc);
   }
@@ -669,15 +704,75 @@ __global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
 // back projection: kernel `radon_ad` (3-D :818-844): linear interpolation
 // between detector bins floor(t) and floor(t)+1 at t = dot((x, y, 1, 0), ofs[j]).
 // ===========================================================================
-template <int VW>
+template <int VW, bool EXACT = true, int AU = 1>
 __device__ __forceinline__ void radon_ad_pixel(const float *__restrict__ lam, size_t S, int nd, int nang,
                                                const float4 *__restrict__ ofs, float xf, float yf,
                                                const Slices<VW> &sl, float (&acc)[VW]) {
 #pragma unroll
   for (int k = 0; k < VW; ++k) acc[k] = 0.f;
   const float fnd = (float)nd;
+  int j = 0;
+  if constexpr (AU == 1) {
+    // one angle at a time, taps accumulated as they arrive (the compiler overlaps
+    // consecutive angles)
 #pragma unroll 2
-  for (int j = 0; j < nang; ++j) {
+    for (; j < nang; ++j) {
+      const float4 o = __ldg(ofs + j);
+      const float tt = __fadd_rn(__fadd_rn(__fmul_rn(xf, o.x), __fmul_rn(yf, o.y)), o.z);
+      if (tt > -1.f && tt < fnd) {
+        const float fl = floorf(tt);
+        const float p = fminf(__fsub_rn(tt, fl), 0x1.fffffep-1f);
+        const float q = __fsub_rn(1.0f, p);
+        const int il = (int)fl;
+        const float *lj = lam + (size_t)j * nd * S;
+        float a[VW], b[VW];
+        if (il >= 0) {
+          sl.load(lj + (size_t)il * S, a);
+#pragma unroll
+          for (int k = 0; k < VW; ++k) acc[k] = EXACT ? __fadd_rn(acc[k], __fmul_rn(q, a[k])) : __fmaf_rn(q, a[k], acc[k]);
+        }
+        if (il <= nd - 2) {
+          sl.load(lj + (size_t)(il + 1) * S, b);
+#pragma unroll
+          for (int k = 0; k < VW; ++k) acc[k] = EXACT ? __fadd_rn(acc[k], __fmul_rn(p, b[k])) : __fmaf_rn(p, b[k], acc[k]);
+        }
+      }
+    }
+  } else {
+  // AU angles per step: their taps are loaded together, then accumulated in angle order
+  for (; j + AU <= nang; j += AU) {
+    int il[AU];
+    float p[AU];
+    bool ta[AU], tb[AU];
+    float a[AU][VW], b[AU][VW];
+#pragma unroll
+    for (int u = 0; u < AU; ++u) {
+      const float4 o = __ldg(ofs + j + u);
+      const float tt = __fadd_rn(__fadd_rn(__fmul_rn(xf, o.x), __fmul_rn(yf, o.y)), o.z);
+      const bool in = tt > -1.f && tt < fnd;
+      const float fl = floorf(tt);
+      p[u] = fminf(__fsub_rn(tt, fl), 0x1.fffffep-1f);
+      il[u] = (int)fl;
+      ta[u] = in && il[u] >= 0;
+      tb[u] = in && il[u] <= nd - 2;
+      const float *lj = lam + (size_t)(j + u) * nd * S;
+      if (ta[u]) sl.load(lj + (size_t)il[u] * S, a[u]);
+      if (tb[u]) sl.load(lj + (size_t)(il[u] + 1) * S, b[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < AU; ++u) {
+      const float q = __fsub_rn(1.0f, p[u]);
+      if (ta[u]) {
+#pragma unroll
+        for (int k = 0; k < VW; ++k) acc[k] = EXACT ? __fadd_rn(acc[k], __fmul_rn(q, a[u][k])) : __fmaf_rn(q, a[u][k], acc[k]);
+      }
+      if (tb[u]) {
+#pragma unroll
+        for (int k = 0; k < VW; ++k) acc[k] = EXACT ? __fadd_rn(acc[k], __fmul_rn(p[u], b[u][k])) : __fmaf_rn(p[u], b[u][k], acc[k]);
+      }
+    }
+  }
+  for (; j < nang; ++j) {
     const float4 o = __ldg(ofs + j);
     const float tt = __fadd_rn(__fadd_rn(__fmul_rn(xf, o.x), __fmul_rn(yf, o.y)), o.z);
     if (tt > -1.f && tt < fnd) {
@@ -690,13 +785,99 @@ __device__ __forceinline__ void radon_ad_pixel(const float *__restrict__ lam, si
       if (il >= 0) {
         sl.load(lj + (size_t)il * S, a);
 #pragma unroll
-        for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(q, a[k]));
+        for (int k = 0; k < VW; ++k) acc[k] = EXACT ? __fadd_rn(acc[k], __fmul_rn(q, a[k])) : __fmaf_rn(q, a[k], acc[k]);
       }
       if (il <= nd - 2) {
         sl.load(lj + (size_t)(il + 1) * S, b);
 #pragma unroll
-        for (int k = 0; k < VW; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(p, b[k]));
+        for (int k = 0; k < VW; ++k) acc[k] = EXACT ? __fadd_rn(acc[k], __fmul_rn(p, b[k])) : __fmaf_rn(p, b[k], acc[k]);
       }
+    }
+  }
+  }
+}
+
+// Back-projection table: per (pixel, angle) the detector bin floor(t) and the
+// interpolation fraction p of radon_ad (3-D :832-839), computed once per problem
+// with the reference's arithmetic; il = INT_MIN marks t outside (-1, nd).
+__global__ void k_bp_table(const float4 *__restrict__ ofs, int N, int nd, int nang, int2 *__restrict__ tab) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)N * N * nang) return;
+  const int pix = (int)(t / nang), j = (int)(t - (long long)pix * nang);
+  const int y = pix / N, x = pix - y * N;
+  const float4 o = __ldg(ofs + j);
+  const float tt = __fadd_rn(__fadd_rn(__fmul_rn((float)x, o.x), __fmul_rn((float)y, o.y)), o.z);
+  int2 e = make_int2(INT_MIN, 0);
+  if (tt > -1.f && tt < (float)nd) {
+    const float fl = floorf(tt);
+    e = make_int2((int)fl, __float_as_int(fminf(__fsub_rn(tt, fl), 0x1.fffffep-1f)));
+  }
+  tab[t] = e;
+}
+
+template <int VW, bool EXACT>
+__device__ __forceinline__ void bp_tap(float (&acc)[VW], float w, const float (&v)[VW]) {
+#pragma unroll
+  for (int k = 0; k < VW; ++k) acc[k] = mac<EXACT>(acc[k], w, v[k]);
+}
+
+template <int VW, bool EXACT, int AU>
+__device__ __forceinline__ void radon_ad_table(const float *__restrict__ lam, size_t S, int nd, int nang,
+                                               const int2 *__restrict__ tab, const Slices<VW> &sl,
+                                               float (&acc)[VW]) {
+#pragma unroll
+  for (int k = 0; k < VW; ++k) acc[k] = 0.f;
+  const size_t jstride = (size_t)nd * S;
+  int j = 0;
+  if (AU == 2) {
+    for (; j + 2 <= nang; j += 2) {  // two angles (four taps) in flight, accumulated in order
+      const int2 e0 = __ldg(tab + j), e1 = __ldg(tab + j + 1);
+      float a0[VW], b0[VW], a1[VW], b1[VW];
+      const float *l0 = lam + (size_t)j * jstride, *l1 = l0 + jstride;
+      const bool in0 = e0.x != INT_MIN, in1 = e1.x != INT_MIN;
+      const bool ta0 = in0 && e0.x >= 0, tb0 = in0 && e0.x <= nd - 2;
+      const bool ta1 = in1 && e1.x >= 0, tb1 = in1 && e1.x <= nd - 2;
+      if (ta0) sl.load(l0 + (size_t)e0.x * S, a0);
+      if (tb0) sl.load(l0 + (size_t)(e0.x + 1) * S, b0);
+      if (ta1) sl.load(l1 + (size_t)e1.x * S, a1);
+      if (tb1) sl.load(l1 + (size_t)(e1.x + 1) * S, b1);
+      const float p0 = __int_as_float(e0.y), p1 = __int_as_float(e1.y);
+      if (ta0) bp_tap<VW, EXACT>(acc, __fsub_rn(1.0f, p0), a0);
+      if (tb0) bp_tap<VW, EXACT>(acc, p0, b0);
+      if (ta1) bp_tap<VW, EXACT>(acc, __fsub_rn(1.0f, p1), a1);
+      if (tb1) bp_tap<VW, EXACT>(acc, p1, b1);
+    }
+  }
+  for (; AU > 2 && j + AU <= nang; j += AU) {  // AU angles (2 AU taps) in flight, accumulated in order
+    int2 e[AU];
+#pragma unroll
+    for (int u = 0; u < AU; ++u) e[u] = __ldg(tab + j + u);
+    float a[AU][VW], b[AU][VW];
+    bool ta[AU], tb[AU];
+#pragma unroll
+    for (int u = 0; u < AU; ++u) {
+      const bool in = e[u].x != INT_MIN;
+      ta[u] = in && e[u].x >= 0;
+      tb[u] = in && e[u].x <= nd - 2;
+      const float *l = lam + (size_t)(j + u) * jstride;
+      if (ta[u]) sl.load(l + (size_t)e[u].x * S, a[u]);
+      if (tb[u]) sl.load(l + (size_t)(e[u].x + 1) * S, b[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < AU; ++u) {
+      const float p = __int_as_float(e[u].y);
+      if (ta[u]) bp_tap<VW, EXACT>(acc, __fsub_rn(1.0f, p), a[u]);
+      if (tb[u]) bp_tap<VW, EXACT>(acc, p, b[u]);
+    }
+  }
+  for (; j < nang; ++j) {
+    const int2 e0 = __ldg(tab + j);
+    if (e0.x != INT_MIN) {
+      const float *l0 = lam + (size_t)j * jstride;
+      const float p0 = __int_as_float(e0.y);
+      float a0[VW], b0[VW];
+      if (e0.x >= 0) { sl.load(l0 + (size_t)e0.x * S, a0); bp_tap<VW, EXACT>(acc, __fsub_rn(1.0f, p0), a0); }
+      if (e0.x <= nd - 2) { sl.load(l0 + (size_t)(e0.x + 1) * S, b0); bp_tap<VW, EXACT>(acc, p0, b0); }
     }
   }
 }
@@ -793,26 +974,38 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
   }
 }
 
-// k_primal: radon_ad of lambda, then the primal update of each chunk of slices.
-template <int DIM, bool TGV, int VW>
-__global__ void __launch_bounds__(256) k_primal(const IterParams P) {
+// k_bp: back projection K* lambda of every (pixel, slice) into P.kstar; it only
+// needs lambda, so it runs beside k_dual.
+template <int VW, int AU, bool TAB>
+__global__ void __launch_bounds__(256) k_bp(const IterParams P) {
   const Dims d = P.d;
   long long unit;
   Slices<VW> sl;
   if (!map_thread<VW>((long long)d.N * d.N, d.S, unit, sl)) return;
   const int pix = (int)unit;
-  const int y = pix / d.N, x = pix - y * d.N;
-  float kstar[VW];
-  radon_ad_pixel<VW>(P.lam, d.S, d.nd, d.nang, P.ofs, (float)x, (float)y, sl, kstar);
-  if (VW == 8) {
-    float ka[4], kb[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) { ka[k] = kstar[k]; kb[k] = kstar[(4 + k) % VW]; }
-    if (sl.va) primal_update<DIM, TGV, 4>(P, x, y, sl.s0, ka);
-    if (sl.vb) primal_update<DIM, TGV, 4>(P, x, y, sl.s0 + 128, kb);
+  float acc[VW];
+  if (TAB && P.bp_tab) {
+    radon_ad_table<VW, false, AU>(P.lam, d.S, d.nd, d.nang, P.bp_tab + (size_t)pix * d.nang, sl, acc);
   } else {
-    primal_update<DIM, TGV, VW>(P, x, y, sl.s0, kstar);
+    const int y = pix / d.N, x = pix - y * d.N;
+    radon_ad_pixel<VW, false, AU>(P.lam, d.S, d.nd, d.nang, P.ofs, (float)x, (float)y, sl, acc);
   }
+  sl.store(P.kstar + (size_t)pix * d.S, acc);
+}
+
+// k_update: update_u + update_p + extrapolation for UW consecutive slices.
+template <int DIM, bool TGV, int UW>
+__global__ void __launch_bounds__(256) k_update(const IterParams P) {
+  const Dims d = P.d;
+  const int nsg = d.S / UW;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)d.N * d.N * nsg) return;
+  const int pix = (int)(t / nsg);
+  const int s0 = (int)(t - (long long)pix * nsg) * UW;
+  const int y = pix / d.N, x = pix - y * d.N;
+  float ks[UW];
+  ldw<UW>(P.kstar + (size_t)pix * d.S + s0, ks);
+  primal_update<DIM, TGV, UW>(P, x, y, s0, ks);
 }
 
 // ===========================================================================
@@ -979,38 +1172,82 @@ cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st) 
 // slices per lane: 8 (two float4 chunks) when S is a multiple of 4, else 2, else 1
 static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 : 1); }
 
-template <int VW>
+// Tunable launch shapes of the projector kernels (chosen per problem shape by
+// the autotuner in gt_api.cu).  S a multiple of 4: k_fwd configs 0..3 =
+// (slices per lane, ray-table entries in flight) = (8, 4), (8, 8), (4, 4), (4, 8);
+// k_bp configs 0..7 = (slices per lane, angles per step, geometry) = (8, 2, table),
+// (8, 4, table), (4, 2, table), (4, 4, table), (8, 1, on the fly), (4, 1, on the fly),
+// (8, 2, on the fly), (4, 2, on the fly).
+// Otherwise one fixed shape with 2 or 1 slices per thread.
+int num_proj_configs(int S, int which) { return S % 4 == 0 ? (which == 0 ? 4 : 8) : 1; }
+
+template <int VW, int UNR>
 static void fwd_vw(const IterParams &P, int disc, cudaStream_t st) {
   const unsigned g = blocks_for(threads_for<VW>((long long)P.d.nd * P.d.nang, P.d.S), 256);
-  if (disc == KL) k_fwd<KL, VW><<<g, 256, 0, st>>>(P);
-  else k_fwd<L2, VW><<<g, 256, 0, st>>>(P);
+  if (disc == KL) k_fwd<KL, VW, UNR><<<g, 256, 0, st>>>(P);
+  else k_fwd<L2, VW, UNR><<<g, 256, 0, st>>>(P);
 }
 
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
-  const int vw = vec_width(P.d.S);
-  if (vw == 8) fwd_vw<8>(P, disc, st);
-  else if (vw == 2) fwd_vw<2>(P, disc, st);
-  else fwd_vw<1>(P, disc, st);
+  const int S = P.d.S;
+  if (S % 4 == 0) {
+    switch (P.fwd_cfg) {
+      case 1: fwd_vw<8, 8>(P, disc, st); break;
+      case 2: fwd_vw<4, 4>(P, disc, st); break;
+      case 3: fwd_vw<4, 8>(P, disc, st); break;
+      default: fwd_vw<8, 4>(P, disc, st); break;
+    }
+  } else if (S % 2 == 0) {
+    fwd_vw<2, 4>(P, disc, st);
+  } else {
+    fwd_vw<1, 4>(P, disc, st);
+  }
   return cudaGetLastError();
 }
 
-template <int VW>
-static void primal_vw(const IterParams &P, int tgv, cudaStream_t st) {
-  const unsigned g = blocks_for(threads_for<VW>((long long)P.d.N * P.d.N, P.d.S), 256);
-  if (P.d.dim == 3) {
-    if (tgv) k_primal<3, true, VW><<<g, 256, 0, st>>>(P);
-    else k_primal<3, false, VW><<<g, 256, 0, st>>>(P);
+template <int VW, int AU, bool TAB = true>
+static void bp_vw(const IterParams &P, cudaStream_t st) {
+  k_bp<VW, AU, TAB><<<blocks_for(threads_for<VW>((long long)P.d.N * P.d.N, P.d.S), 256), 256, 0, st>>>(P);
+}
+
+cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
+  const int S = P.d.S;
+  if (S % 4 == 0) {
+    switch (P.bp_cfg) {
+      case 1: bp_vw<8, 4>(P, st); break;
+      case 2: bp_vw<4, 2>(P, st); break;
+      case 3: bp_vw<4, 4>(P, st); break;
+      case 4: bp_vw<8, 1, false>(P, st); break;
+      case 5: bp_vw<4, 1, false>(P, st); break;
+      case 6: bp_vw<8, 2, false>(P, st); break;
+      case 7: bp_vw<4, 2, false>(P, st); break;
+      default: bp_vw<8, 2>(P, st); break;
+    }
+  } else if (S % 2 == 0) {
+    bp_vw<2, 2>(P, st);
   } else {
-    if (tgv) k_primal<2, true, VW><<<g, 256, 0, st>>>(P);
-    else k_primal<2, false, VW><<<g, 256, 0, st>>>(P);
+    bp_vw<1, 2>(P, st);
+  }
+  return cudaGetLastError();
+}
+
+template <int UW>
+static void update_uw(const IterParams &P, int tgv, cudaStream_t st) {
+  const unsigned g = blocks_for((long long)P.d.N * P.d.N * (P.d.S / UW), 256);
+  if (P.d.dim == 3) {
+    if (tgv) k_update<3, true, UW><<<g, 256, 0, st>>>(P);
+    else k_update<3, false, UW><<<g, 256, 0, st>>>(P);
+  } else {
+    if (tgv) k_update<2, true, UW><<<g, 256, 0, st>>>(P);
+    else k_update<2, false, UW><<<g, 256, 0, st>>>(P);
   }
 }
 
-cudaError_t launch_primal(const IterParams &P, int tgv, cudaStream_t st) {
-  const int vw = vec_width(P.d.S);
-  if (vw == 8) primal_vw<8>(P, tgv, st);
-  else if (vw == 2) primal_vw<2>(P, tgv, st);
-  else primal_vw<1>(P, tgv, st);
+cudaError_t launch_update(const IterParams &P, int tgv, cudaStream_t st) {
+  const int S = P.d.S;
+  if (S % 4 == 0) update_uw<4>(P, tgv, st);
+  else if (S % 2 == 0) update_uw<2>(P, tgv, st);
+  else update_uw<1>(P, tgv, st);
   return cudaGetLastError();
 }
 
@@ -1051,6 +1288,11 @@ cudaError_t launch_ray_count(const float4 *ofs, int N, int nd, int nang, int *co
 cudaError_t launch_ray_fill(const float4 *ofs, int N, int nd, int nang, const long long *start, int2 *ent,
                             cudaStream_t st) {
   k_ray_fill<<<blocks_for((long long)nd * nang, 128), 128, 0, st>>>(ofs, N, nd, nang, start, ent);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_table(const float4 *ofs, int N, int nd, int nang, int2 *tab, cudaStream_t st) {
+  k_bp_table<<<blocks_for((long long)N * N * nang, 256), 256, 0, st>>>(ofs, N, nd, nang, tab);
   return cudaGetLastError();
 }
 

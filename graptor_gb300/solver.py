@@ -39,7 +39,8 @@ class Problem:
     """
 
     def __init__(self, dim, N, Nz, C, nd, angles, alpha=(4.0, 1.0), mu=None, discrepancy="KL",
-                 regularisation="TGV", coupling="FROB", stepsize=1.0, normest=None, device=0, stream=None):
+                 regularisation="TGV", coupling="FROB", stepsize=1.0, normest=None, device=0, stream=None,
+                 autotune=True):
         self._h = None
         self.dim, self.N, self.Nz, self.C, self.nd = int(dim), int(N), int(Nz), int(C), int(nd)
         self.angles = np.ascontiguousarray(angles, dtype=np.float64)
@@ -66,6 +67,7 @@ class Problem:
         d.normest = float(normest) if normest else 0.0
         d.device = int(device)
         d.stream = stream
+        d.autotune = int(bool(autotune))
         h = ctypes.c_void_p()
         L.check(L.lib().gt_problem_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h
@@ -123,6 +125,13 @@ class Problem:
         L.check(L.lib().gt_get_scalars(self._h, out))
         return {"normest": out[0], "sigma": out[1], "tau": out[2], "iterations": int(out[3])}
 
+    @property
+    def tuning(self) -> dict:
+        """Projector launch shapes the autotuner chose (see launch_fwd / launch_bp)."""
+        out = (ctypes.c_int * 2)()
+        L.check(L.lib().gt_get_tuning(self._h, out))
+        return {"fwd_cfg": out[0], "bp_cfg": out[1]}
+
     def gap(self) -> dict:
         out = (ctypes.c_double * 4)()
         L.check(L.lib().gt_gap(self._h, out))
@@ -130,9 +139,9 @@ class Problem:
 
     def time_kernels(self, reps: int = 5) -> dict:
         """Mean CUDA-event duration (ms) of each kernel of one iteration."""
-        out = (ctypes.c_float * 3)()
-        L.check(L.lib().gt_time_kernels(self._h, int(reps), out, 3))
-        return {"k_dual": out[0], "k_fwd": out[1], "k_primal": out[2]}
+        out = (ctypes.c_float * 4)()
+        L.check(L.lib().gt_time_kernels(self._h, int(reps), out, 4))
+        return {"k_dual": out[0], "k_fwd": out[1], "k_bp": out[2], "k_update": out[3]}
 
     @property
     def launches_per_iteration(self) -> int:

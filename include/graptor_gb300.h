@@ -73,6 +73,7 @@ typedef struct gt_desc {
   double normest;       /* > 0: use this operator-norm estimate; <= 0: FP64 power iteration on device */
   int device;           /* CUDA device ordinal */
   void *stream;         /* cudaStream_t to run on, or NULL for a library-owned stream */
+  int autotune;         /* != 0: time the projector launch shapes at gt_set_data and keep the fastest */
 } gt_desc;
 
 typedef struct gt_problem gt_problem;
@@ -97,6 +98,10 @@ GT_API int gt_synchronize(gt_problem *p);
 GT_API int gt_get_state(gt_problem *p, int field, float *host);
 GT_API int gt_set_state(gt_problem *p, int field, const float *host);
 
+/* Launch shapes the autotuner chose: [0] forward projector, [1] back projector
+ * (indices into the configurations listed at launch_fwd / launch_bp). */
+GT_API int gt_get_tuning(gt_problem *p, int out[2]);
+
 /* Scalars the run uses: [0] normest, [1] sigma, [2] tau, [3] iterations run. */
 GT_API int gt_get_scalars(gt_problem *p, double out[4]);
 
@@ -113,10 +118,10 @@ GT_API int gt_radon(const float *img_dev, float *sino_dev, const double *angles,
 GT_API int gt_radon_ad(const float *sino_dev, float *img_dev, const double *angles, int N, int nd, int nang, int S,
                 void *stream);
 
-/* Run reps iterations kernel by kernel (not graph-captured), timing each kernel
- * with CUDA events on the problem stream; ms_out[0..2] receive the mean duration
- * of k_dual, k_fwd and k_primal (n >= 3).  The iterations are real: the state
- * advances by reps iterations. */
+/* Run reps iterations kernel by kernel (not graph-captured, no overlap), timing
+ * each kernel with CUDA events on the problem stream; ms_out[0..3] receive the
+ * mean duration of k_dual, k_fwd, k_bp and k_update (n >= 4).  The iterations are
+ * real: the state advances by reps iterations. */
 GT_API int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n);
 
 /* Number of kernel launches one iteration issues (for launch accounting). */
