@@ -62,6 +62,8 @@ _SIGS = {
     "gt_radon_ad": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "gt_launches_per_iteration": (ctypes.c_int, [_P]),
     "gt_time_kernels": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    "gt_normest_noalloc": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P,
+                                          ctypes.POINTER(ctypes.c_double)]),
     "gt_last_error": (ctypes.c_char_p, []),
     "gt_version": (ctypes.c_char_p, []),
 }

@@ -263,6 +263,12 @@ int autotune(gt_problem *p) {
 
 }  // namespace
 
+// error reporting for the library's other translation units
+namespace gt {
+int set_error(int code, const char *msg) { return set_err(code, "%s", msg); }
+int cuda_error(cudaError_t e, const char *what, int line) { return cuda_err(e, what, line); }
+}  // namespace gt
+
 extern "C" {
 
 const char *gt_last_error(void) { return g_err.c_str(); }

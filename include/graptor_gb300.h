@@ -124,6 +124,23 @@ GT_API int gt_radon_ad(const float *sino_dev, float *img_dev, const double *angl
  * real: the state advances by reps iterations. */
 GT_API int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n);
 
+/* Allocation-free operator-norm estimate.  No counterpart in the reference (which
+ * estimates the norm inside tgv_radon with freshly allocated buffers).
+ *
+ * For callers that cannot allocate device memory while they run -- code inside a
+ * host framework that owns the device memory (its pool or caching allocator), or
+ * latency-sensitive code that cannot afford cudaFree's device-wide
+ * synchronisation.  It runs the FP64 power iteration of gt_set_data (normest <= 0)
+ * for the geometry (angles, N, nd, nang) on `device` / `stream` and writes the
+ * estimate to *out, without cudaMalloc, cudaFree or any other allocation: its
+ * scratch is a fixed 8 MiB device array inside the library (kept by every GPU
+ * that loads the library until the process exits).
+ * Limit: 4*nang + N*N + nd*nang + 256 <= 1048576 (doubles); larger geometries
+ * return GT_ERR_ARG.  Calls share the scratch, so calls whose GPU work overlaps
+ * race; serialise them.  The first call on a device sets up the scratch address
+ * for that device: make it before any stream capture. */
+GT_API int gt_normest_noalloc(const double *angles, int N, int nd, int nang, int device, void *stream, double *out);
+
 /* Number of kernel launches one iteration issues (for launch accounting). */
 GT_API int gt_launches_per_iteration(const gt_problem *p);
 
