@@ -58,6 +58,7 @@ _SIGS = {
     "gt_get_scalars": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
     "gt_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     "gt_gap": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "gt_gap_ex": (ctypes.c_int, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
     "gt_radon": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "gt_radon_ad": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "gt_launches_per_iteration": (ctypes.c_int, [_P]),

@@ -39,6 +39,11 @@ cudaError_t launch_ray_fill(const float4 *ofs, int N, int nd, int nang, const lo
                             cudaStream_t st);
 cudaError_t launch_bp_table(const float4 *ofs, int N, int nd, int nang, int2 *tab, cudaStream_t st);
 int num_proj_configs(int S, int which);
+int gap_blocks(const IterParams &P);
+cudaError_t launch_gap_pass1(const IterParams &P, int disc, int tgv, int cpl, float *vt, double *part, int nb,
+                             cudaStream_t st);
+cudaError_t launch_gap_pass2(const IterParams &P, const float *vt, double theta, double U, double *part, int nb,
+                             cudaStream_t st);
 }  // namespace gt
 
 namespace {
@@ -112,6 +117,8 @@ struct gt_problem {
   float *lam = nullptr, *f = nullptr, *ku = nullptr, *stage = nullptr, *kstar = nullptr;
   void *rays = nullptr;        // ray table (offsets + entries), built at creation
   size_t ray_bytes = 0;
+  void *gap_ws = nullptr;      // gap workspace (v~ planes + FP64 block partials), allocated on first gt_gap
+  double *mu64 = nullptr;
   gt::IterParams P{};
   bool autotune = true;
   cudaGraphExec_t g_one = nullptr, g_chunk = nullptr;
@@ -339,7 +346,8 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
       tgv ? align256(fv * p->KW) : 0,                               // w
       align256(fb), align256(fb), align256(fb),                     // lam, f, ku
       align256(std::max(fv, fb)),                                   // stage
-      align256(fv)};                                                // kstar
+      align256(fv),                                                 // kstar
+      align256(sizeof(double) * D.C)};                              // mu (double)
   const int nsz = (int)(sizeof(sizes) / sizeof(sizes[0]));
   for (int k = 0; k < nsz; ++k) { off[k] = total; total += sizes[k]; }
   cudaError_t e = cudaMalloc(&p->block, total);
@@ -363,6 +371,7 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
   p->ku = (float *)(b + off[11]);
   p->stage = (float *)(b + off[12]);
   p->kstar = (float *)(b + off[13]);
+  p->mu64 = (double *)(b + off[14]);
 
   std::vector<float> t32((size_t)D.nang * 4);
   for (size_t k = 0; k < t32.size(); ++k) t32[k] = (float)p->ofs64h[k];
@@ -412,7 +421,7 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
   P.d = p->d;
   P.ofs = p->ofs; P.mu = p->mu_eff;
   P.u = p->u; P.ubar = p->ubar; P.p = p->p; P.pbar = p->pbar; P.v = p->v; P.w = p->w;
-  P.lam = p->lam; P.f = p->f; P.ku = p->ku; P.kstar = p->kstar;
+  P.lam = p->lam; P.f = p->f; P.ku = p->ku; P.kstar = p->kstar; P.mu64 = p->mu64;
   *out = p;
   return GT_OK;
 }
@@ -425,6 +434,7 @@ void gt_problem_destroy(gt_problem *p) {
   if (p->g_chunk) cudaGraphExecDestroy(p->g_chunk);
   if (p->block) cudaFree(p->block);
   if (p->rays) cudaFree(p->rays);
+  if (p->gap_ws) cudaFree(p->gap_ws);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
   if (p->side) cudaStreamDestroy(p->side);
@@ -471,6 +481,8 @@ int gt_set_data(gt_problem *p, const float *f_host, int make_feasible) {
   for (int c = 0; c < d.C; ++c)
     me[c] = (float)(p->disc == GT_KL ? p->mu[c] : p->mu[c] / (p->sigma + p->mu[c]));
   CK(cudaMemcpyAsync(p->mu_eff, me.data(), sizeof(float) * d.C, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(p->mu64, p->mu.data(), sizeof(double) * d.C, cudaMemcpyHostToDevice, p->stream));
+  p->P.ne64 = p->ne;
   // pick the projector launch shapes (uses lambda / ku / kstar as scratch: they are reset below)
   {
     const int rc = autotune(p);
@@ -563,9 +575,51 @@ int gt_get_scalars(gt_problem *p, double out[4]) {
   return GT_OK;
 }
 
+int gt_gap_ex(gt_problem *p, double U, double out[8]) {
+  if (!p || !out) return set_err(GT_ERR_ARG, "null argument");
+  if (!p->has_data) return set_err(GT_ERR_STATE, "gt_gap before gt_set_data");
+  CK(cudaSetDevice(p->device));
+  const bool tgv = p->reg == GT_TGV;
+  const int nb = gt::gap_blocks(p->P);
+  const size_t vt_bytes = tgv ? align256(sizeof(float) * p->d.vol * p->K) : 0;
+  if (!p->gap_ws) {
+    cudaError_t e = cudaMalloc(&p->gap_ws, vt_bytes + sizeof(double) * 7 * (size_t)nb);
+    if (e != cudaSuccess) { p->gap_ws = nullptr; return cuda_err(e, "cudaMalloc (gap workspace)", __LINE__); }
+  }
+  float *vt = tgv ? (float *)p->gap_ws : p->v;
+  double *part = (double *)((char *)p->gap_ws + vt_bytes);
+  std::vector<double> h(7 * (size_t)nb);
+  // K* lambda of the current lambda (k_bp writes only that buffer); the passes
+  // write only their own blocks' partials, so the buffer starts at zero
+  CK(gt::launch_bp(p->P, p->stream));
+  CK(cudaMemsetAsync(part, 0, sizeof(double) * 7 * (size_t)nb, p->stream));
+  CK(gt::launch_gap_pass1(p->P, p->disc, tgv, p->cpl, vt, part, nb, p->stream));
+  CK(cudaMemcpyAsync(h.data(), part, sizeof(double) * 6 * nb, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  auto sum = [&](int q) { double a = 0; for (int k = 0; k < nb; ++k) a += h[(size_t)q * nb + k]; return a; };
+  auto mx = [&](int q) { double a = 0; for (int k = 0; k < nb; ++k) a = std::max(a, h[(size_t)q * nb + k]); return a; };
+  const double ne = p->ne, a0 = p->alpha0 / (ne * ne), a1 = p->alpha1 / (ne * ne);
+  const double data = sum(0) / (p->disc == GT_KL ? ne : ne * ne), fstar = sum(1) / (p->disc == GT_KL ? ne : 1.0);
+  const double reg1 = sum(2), reg0 = tgv ? sum(3) : 0.0, maxv = mx(4), maxu = mx(5);
+  const double theta = maxv > 0 ? std::min(1.0, a1 / maxv) : 1.0;
+  if (!(U > 0)) U = maxu > 0 ? 2.0 * maxu : 1.0;
+  CK(gt::launch_gap_pass2(p->P, vt, theta, U, part, nb, p->stream));
+  CK(cudaMemcpyAsync(h.data() + 6 * (size_t)nb, part + 6 * (size_t)nb, sizeof(double) * nb, cudaMemcpyDeviceToHost,
+                     p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  const double box = sum(6);
+  const double P = a1 * reg1 + a0 * reg0 + data, Dv = -fstar + box;
+  out[0] = P; out[1] = Dv; out[2] = P - Dv; out[3] = (P - Dv) / std::fabs(P);
+  out[4] = theta; out[5] = U; out[6] = data; out[7] = fstar;
+  return GT_OK;
+}
+
 int gt_gap(gt_problem *p, double out[4]) {
-  (void)p; (void)out;
-  return set_err(GT_ERR_STATE, "gt_gap: not available in this build");
+  double o[8];
+  const int rc = gt_gap_ex(p, 0.0, o);
+  if (rc) return rc;
+  for (int k = 0; k < 4; ++k) out[k] = o[k];
+  return GT_OK;
 }
 
 int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n) {

@@ -52,6 +52,8 @@ struct IterParams {
   float *w;              // [KW][vol]
   float *lam, *f, *ku;   // [nbin]
   float *kstar;          // [vol] back projection K* lambda
+  const double *mu64;    // [C] mu (KL) or mu (L2) in double, for the gap
+  double ne64;           // operator-norm estimate, for the gap
 };
 
 }  // namespace gt

@@ -15,6 +15,7 @@
 // k_dual and the chain k_fwd -> k_bp read only what the previous k_update wrote
 // and write disjoint fields, so they run concurrently.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <climits>
 #include <math.h>
 
@@ -1134,6 +1135,241 @@ __global__ void k_scale64(double *__restrict__ x, size_t n, const double *__rest
 }
 
 // ===========================================================================
+// FP64 primal-dual gap of the current iterate (no counterpart in the reference's
+// loop; its draft energy code is radon_tgv_primal_dual_3d.py:882-927).  Problem:
+//   P = a1~ sum_x |grad u - p|_V + a0~ sum_x |E p|_W* + D(u),  u in [0, U]
+//   D = -F~*(lam) + U sum min(0, K^T lam - theta div v~),  v~ = -div_sym w
+// Per-block FP64 partial sums / maxima; the host reduces the blocks in order.
+// ===========================================================================
+enum { GQ_DATA = 0, GQ_FSTAR, GQ_REG1, GQ_REG0, GQ_MAXV, GQ_MAXU, GQ_BOX, GQ_N };
+
+__device__ __forceinline__ void block_reduce_store(double v, bool is_max, double *out) {
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    const double t = __shfl_down_sync(0xffffffffu, v, o);
+    v = is_max ? fmax(v, t) : v + t;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : (is_max ? -1e300 : 0.0);
+    for (int o = 16; o > 0; o >>= 1) {
+      const double t = __shfl_down_sync(0xffffffffu, v, o);
+      v = is_max ? fmax(v, t) : v + t;
+    }
+    if (lane == 0) out[blockIdx.x] = v;
+  }
+}
+
+// data term and conjugate per bin: R u from the ray table (FP32 sum), terms in FP64
+template <int DISC>
+__global__ void __launch_bounds__(256) k_gap_data(const IterParams P, double *part_data, double *part_fstar) {
+  const Dims d = P.d;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double data = 0.0, fs = 0.0;
+  if (t < (long long)d.nbin) {
+    const int b = (int)(t / d.S), s = (int)(t - (long long)b * d.S);
+    const long long r0 = P.ray_start[b], r1 = P.ray_start[b + 1];
+    float acc = 0.f;
+    for (long long e = r0; e < r1; ++e) {
+      const int2 en = P.ray_ent[e];
+      acc = __fmaf_rn(__int_as_float(en.y), P.u[(size_t)en.x * d.S + s], acc);
+    }
+    const double Ru = acc, f = P.f[t], lam = P.lam[t];
+    const double m = P.mu64[s / d.Nz];
+    if (DISC == KL) {
+      if (f > 0.0) {
+        data = m * (Ru - f + f * log(f / Ru));  // +inf where R u = 0 < f
+        fs = -m * f * log1p(-lam / m);
+      } else {
+        data = m * Ru;
+      }
+    } else {
+      data = 0.5 * m * (Ru - f) * (Ru - f);   // the host divides by ne^2
+      fs = lam * f / P.ne64 + 0.5 * lam * lam / m;
+    }
+  }
+  block_reduce_store(data, false, part_data);
+  block_reduce_store(fs, false, part_fstar);
+}
+
+// support of the ball {sum b w^2 <= 1} under <w, e> = sum m w e  -> weights m^2/b
+template <int DIM, int CPL>
+__device__ __forceinline__ double wsupport_weight(int k) {
+  const double q = 1.4142 * 1.4142;
+  if (DIM == 3) {
+    if (k < 3) return 1.0;
+    if (CPL == UNCORR && k == 5) return 4.0;
+    return 4.0 / q;
+  }
+  if (k < 2) return 1.0;
+  return CPL == UNCORR ? 4.0 / q : 1.0;
+}
+
+// singular values of the C x K matrix with Gram matrix G (K = 2 or 3), via the
+// eigenvalues of G: 2x2 closed form, 3x3 trigonometric form for symmetric matrices
+__device__ __forceinline__ void gram_singular(int K, const double G[6], double sv[3]) {
+  if (K == 2) {
+    const double a = G[0], b = G[1], c = G[2];
+    const double tr = a + c, dt = sqrt(fmax(0.0, 0.25 * (a - c) * (a - c) + b * b));
+    sv[0] = sqrt(fmax(0.0, 0.5 * tr + dt));
+    sv[1] = sqrt(fmax(0.0, 0.5 * tr - dt));
+    sv[2] = 0.0;
+    return;
+  }
+  // G = [a d e; d b f; e f c] stored (a, b, c, d, e, f)
+  const double a = G[0], b = G[1], c = G[2], dd = G[3], e = G[4], f = G[5];
+  const double p1 = dd * dd + e * e + f * f;
+  const double q = (a + b + c) / 3.0;
+  const double p2 = (a - q) * (a - q) + (b - q) * (b - q) + (c - q) * (c - q) + 2.0 * p1;
+  double l0, l1, l2;
+  if (p2 <= 1e-300) {
+    l0 = l1 = l2 = q;
+  } else {
+    const double pp = sqrt(p2 / 6.0);
+    const double B0 = (a - q) / pp, B1 = (b - q) / pp, B2 = (c - q) / pp, B3 = dd / pp, B4 = e / pp, B5 = f / pp;
+    const double detB = B0 * (B1 * B2 - B5 * B5) - B3 * (B3 * B2 - B5 * B4) + B4 * (B3 * B5 - B1 * B4);
+    const double r = fmin(1.0, fmax(-1.0, 0.5 * detB));
+    const double phi = acos(r) / 3.0;
+    l0 = q + 2.0 * pp * cos(phi);
+    l2 = q + 2.0 * pp * cos(phi + 2.0943951023931957);
+    l1 = 3.0 * q - l0 - l2;
+  }
+  sv[0] = sqrt(fmax(0.0, l0));
+  sv[1] = sqrt(fmax(0.0, l1));
+  sv[2] = sqrt(fmax(0.0, l2));
+}
+
+// per (pixel, z), all channels: regulariser supports, v~ = -div_sym w (stored), max |v~|, max u
+template <int DIM, bool TGV, int CPL, int CMAX>
+__global__ void __launch_bounds__(256) k_gap_vox(const IterParams P, float *vt, double *part_reg1, double *part_reg0,
+                                                 double *part_maxv, double *part_maxu) {
+  constexpr int K = DIM, KW = DIM == 3 ? 6 : 3;
+  const Dims d = P.d;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double reg1 = 0.0, reg0 = 0.0, maxv = 0.0, maxu = 0.0;
+  if (t < (long long)d.N * d.N * d.Nz) {
+    const int pix = (int)(t / d.Nz), z = (int)(t - (long long)pix * d.Nz);
+    const int y = pix / d.N, x = pix - y * d.N;
+    const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
+    const double st = P.stepsize;
+    double G1[6] = {0, 0, 0, 0, 0, 0}, Gv[6] = {0, 0, 0, 0, 0, 0};
+    double n1 = 0.0, n0 = 0.0, nv = 0.0;
+    for (int c = 0; c < d.C; ++c) {
+      const size_t i = (size_t)pix * S + (size_t)c * d.Nz + z;
+      const double u0 = P.u[i];
+      maxu = fmax(maxu, u0);
+      double g[3], pc[3] = {0, 0, 0};
+      g[0] = (x < d.N - 1) ? (double)P.u[i + S] - u0 : 0.0;
+      g[1] = (y < d.N - 1) ? (double)P.u[i + rowS] - u0 : 0.0;
+      if (DIM == 3) g[2] = (z < d.Nz - 1) ? ((double)P.u[i + 1] - u0) / st : 0.0;
+      if (TGV)
+        for (int k = 0; k < K; ++k) { pc[k] = P.p[k * vol + i]; g[k] -= pc[k]; }
+      double sq = 0.0;
+      for (int k = 0; k < K; ++k) sq += g[k] * g[k];
+      if (CPL == UNCORR) reg1 += sqrt(sq); else n1 += sq;
+      if (CPL == NUCL) {
+        G1[0] += g[0] * g[0]; G1[1] += g[1] * g[1]; G1[3] += g[0] * g[1];
+        if (DIM == 3) { G1[2] += g[2] * g[2]; G1[4] += g[0] * g[2]; G1[5] += g[1] * g[2]; }
+      }
+      double v3[3];
+      if (TGV) {
+        // E p (backward differences, zero at index 0) and its support
+        double a[3], bb[3], cz[3] = {0, 0, 0};
+        for (int k = 0; k < K; ++k) {
+          a[k] = x > 0 ? pc[k] - (double)P.p[k * vol + i - S] : 0.0;
+          bb[k] = y > 0 ? pc[k] - (double)P.p[k * vol + i - rowS] : 0.0;
+          if (DIM == 3) cz[k] = z > 0 ? (pc[k] - (double)P.p[k * vol + i - 1]) / st : 0.0;
+        }
+        double e[6];
+        if (DIM == 3) {
+          e[0] = a[0]; e[1] = bb[1]; e[2] = cz[2];
+          e[3] = 0.5 * (a[1] + bb[0]); e[4] = 0.5 * (a[2] + cz[0]); e[5] = 0.5 * (bb[2] + cz[1]);
+        } else {
+          e[0] = a[0]; e[1] = bb[1]; e[2] = 0.5 * (a[1] + bb[0]);
+        }
+        double se = 0.0;
+        for (int k = 0; k < KW; ++k) se += wsupport_weight<DIM, CPL == NUCL ? FROB : CPL>(k) * e[k] * e[k];
+        if (CPL == UNCORR) reg0 += sqrt(se); else n0 += se;
+        // v~ = -div_sym w = E^T w (update_p's divergence with opposite sign)
+        const int rx[3] = {0, DIM == 3 ? 3 : 2, 4}, ry[3] = {DIM == 3 ? 3 : 2, 1, 5}, rz[3] = {4, 5, 2};
+        for (int k = 0; k < K; ++k) {
+          double A = -(double)P.w[rx[k] * vol + i], B = -(double)P.w[ry[k] * vol + i], Cz = 0.0;
+          if (x == 0) A = 0.0;
+          if (x < d.N - 1) A += P.w[rx[k] * vol + i + S];
+          if (y == 0) B = 0.0;
+          if (y < d.N - 1) B += P.w[ry[k] * vol + i + rowS];
+          if (DIM == 3) {
+            Cz = -(double)P.w[rz[k] * vol + i];
+            if (z == 0) Cz = 0.0;
+            if (z < d.Nz - 1) Cz += P.w[rz[k] * vol + i + 1];
+            Cz /= st;
+          }
+          v3[k] = -(A + B + Cz);
+          vt[k * vol + i] = (float)v3[k];
+        }
+      } else {
+        for (int k = 0; k < K; ++k) v3[k] = P.v[k * vol + i];
+      }
+      double sv = 0.0;
+      for (int k = 0; k < K; ++k) sv += v3[k] * v3[k];
+      if (CPL == UNCORR) maxv = fmax(maxv, sqrt(sv)); else nv += sv;
+      if (CPL == NUCL) {
+        Gv[0] += v3[0] * v3[0]; Gv[1] += v3[1] * v3[1]; Gv[3] += v3[0] * v3[1];
+        if (DIM == 3) { Gv[2] += v3[2] * v3[2]; Gv[4] += v3[0] * v3[2]; Gv[5] += v3[1] * v3[2]; }
+      }
+    }
+    if (CPL == FROB) {
+      reg1 += sqrt(n1); reg0 += sqrt(n0); maxv = fmax(maxv, sqrt(nv));
+    } else if (CPL == NUCL) {
+      double s1[3], s2[3];
+      double g1[6] = {G1[0], G1[1], G1[2], G1[3], G1[4], G1[5]}, gv[6] = {Gv[0], Gv[1], Gv[2], Gv[3], Gv[4], Gv[5]};
+      if (DIM == 2) { g1[1] = G1[3]; g1[2] = G1[1]; gv[1] = Gv[3]; gv[2] = Gv[1]; }
+      gram_singular(K, g1, s1);
+      gram_singular(K, gv, s2);
+      reg1 += s1[0] + s1[1] + s1[2];
+      reg0 += sqrt(n0);
+      maxv = fmax(maxv, fmax(s2[0], fmax(s2[1], s2[2])));
+    }
+  }
+  block_reduce_store(reg1, false, part_reg1);
+  block_reduce_store(reg0, false, part_reg0);
+  block_reduce_store(maxv, true, part_maxv);
+  block_reduce_store(maxu, true, part_maxu);
+}
+
+// dual box term per (pixel, s): U * min(0, K^T lam - theta div v~)
+template <int DIM>
+__global__ void __launch_bounds__(256) k_gap_box(const IterParams P, const float *vt, double theta, double U,
+                                                 double *part_box) {
+  const Dims d = P.d;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double box = 0.0;
+  if (t < (long long)d.vol) {
+    const int pix = (int)(t / d.S), s = (int)(t - (long long)pix * d.S);
+    const int y = pix / d.N, x = pix - y * d.N, z = s % d.Nz;
+    const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S, i = (size_t)t;
+    double a = vt[i], b = vt[vol + i];
+    if (x == d.N - 1) a = 0.0;
+    if (x > 0) a -= vt[i - S];
+    if (y == d.N - 1) b = 0.0;
+    if (y > 0) b -= vt[vol + i - rowS];
+    double dv = a + b;
+    if (DIM == 3) {
+      double c = vt[2 * vol + i];
+      if (z == d.Nz - 1) c = 0.0;
+      if (z > 0) c -= vt[2 * vol + i - 1];
+      dv += c / (double)P.stepsize;
+    }
+    const double g = (double)P.kstar[i] / P.ne64 - theta * dv;
+    box = U * fmin(0.0, g);
+  }
+  block_reduce_store(box, false, part_box);
+}
+
+// ===========================================================================
 // host-side launchers
 // ===========================================================================
 static inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -1288,6 +1524,47 @@ cudaError_t launch_ray_count(const float4 *ofs, int N, int nd, int nang, int *co
 cudaError_t launch_ray_fill(const float4 *ofs, int N, int nd, int nang, const long long *start, int2 *ent,
                             cudaStream_t st) {
   k_ray_fill<<<blocks_for((long long)nd * nang, 128), 128, 0, st>>>(ofs, N, nd, nang, start, ent);
+  return cudaGetLastError();
+}
+
+// gap: returns per-quantity block partials in `part` ([GQ_N][nblk_max]); host reduces
+int gap_blocks(const IterParams &P) {
+  const long long a = (long long)P.d.nbin, b = (long long)P.d.N * P.d.N * P.d.Nz, c = (long long)P.d.vol;
+  return (int)blocks_for(std::max(a, std::max(b, c)), 256);
+}
+
+template <int DIM, bool TGV, int CPL>
+static void gap_vox_c(const IterParams &P, float *vt, double *part, int nb, cudaStream_t st) {
+  const unsigned g = blocks_for((long long)P.d.N * P.d.N * P.d.Nz, 256);
+  k_gap_vox<DIM, TGV, CPL, 8><<<g, 256, 0, st>>>(P, vt, part + GQ_REG1 * nb, part + GQ_REG0 * nb,
+                                                 part + GQ_MAXV * nb, part + GQ_MAXU * nb);
+}
+
+template <int DIM, bool TGV>
+static void gap_vox_t(const IterParams &P, int cpl, float *vt, double *part, int nb, cudaStream_t st) {
+  if (cpl == UNCORR) gap_vox_c<DIM, TGV, UNCORR>(P, vt, part, nb, st);
+  else if (cpl == FROB) gap_vox_c<DIM, TGV, FROB>(P, vt, part, nb, st);
+  else gap_vox_c<DIM, TGV, NUCL>(P, vt, part, nb, st);
+}
+
+cudaError_t launch_gap_pass1(const IterParams &P, int disc, int tgv, int cpl, float *vt, double *part, int nb,
+                             cudaStream_t st) {
+  const unsigned gd = blocks_for((long long)P.d.nbin, 256);
+  if (disc == KL) k_gap_data<KL><<<gd, 256, 0, st>>>(P, part + GQ_DATA * nb, part + GQ_FSTAR * nb);
+  else k_gap_data<L2><<<gd, 256, 0, st>>>(P, part + GQ_DATA * nb, part + GQ_FSTAR * nb);
+  if (P.d.dim == 3) {
+    if (tgv) gap_vox_t<3, true>(P, cpl, vt, part, nb, st); else gap_vox_t<3, false>(P, cpl, vt, part, nb, st);
+  } else {
+    if (tgv) gap_vox_t<2, true>(P, cpl, vt, part, nb, st); else gap_vox_t<2, false>(P, cpl, vt, part, nb, st);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gap_pass2(const IterParams &P, const float *vt, double theta, double U, double *part, int nb,
+                             cudaStream_t st) {
+  const unsigned g = blocks_for((long long)P.d.vol, 256);
+  if (P.d.dim == 3) k_gap_box<3><<<g, 256, 0, st>>>(P, vt, theta, U, part + GQ_BOX * nb);
+  else k_gap_box<2><<<g, 256, 0, st>>>(P, vt, theta, U, part + GQ_BOX * nb);
   return cudaGetLastError();
 }
 

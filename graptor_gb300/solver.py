@@ -132,10 +132,24 @@ class Problem:
         L.check(L.lib().gt_get_tuning(self._h, out))
         return {"fwd_cfg": out[0], "bp_cfg": out[1]}
 
-    def gap(self) -> dict:
-        out = (ctypes.c_double * 4)()
-        L.check(L.lib().gt_gap(self._h, out))
-        return {"primal": out[0], "dual": out[1], "gap": out[2], "relative": out[3]}
+    def gap(self, U: float = 0.0) -> dict:
+        """FP64 primal-dual gap of the current iterate on the box u in [0, U] (U <= 0: 2 max u)."""
+        out = (ctypes.c_double * 8)()
+        L.check(L.lib().gt_gap_ex(self._h, float(U), out))
+        return {"primal": out[0], "dual": out[1], "gap": out[2], "relative": out[3], "theta": out[4], "U": out[5],
+                "data": out[6], "fstar": out[7]}
+
+    def solve_to_gap(self, tol: float = 1e-4, check_every: int = 50, max_iters: int = 100000) -> dict:
+        """Iterate until the relative gap is <= tol (checked every `check_every` iterations)."""
+        done = 0
+        g = self.gap()
+        while g["relative"] > tol and done < max_iters:
+            n = min(check_every, max_iters - done)
+            self.run(n)
+            done += n
+            g = self.gap()
+        g["iterations"] = done
+        return g
 
     def time_kernels(self, reps: int = 5) -> dict:
         """Mean CUDA-event duration (ms) of each kernel of one iteration."""

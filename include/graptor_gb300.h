@@ -106,9 +106,19 @@ GT_API int gt_get_tuning(gt_problem *p, int out[2]);
 GT_API int gt_get_scalars(gt_problem *p, double out[4]);
 
 /* FP64 primal-dual gap of the current iterate (the reference has none; draft
- * at 3-D :882-927).  out: [0] primal energy, [1] dual energy, [2] gap P-D,
- * [3] relative gap (P-D)/|P|. */
+ * at 3-D :882-927).  Problem solved by the loop (ne = operator-norm estimate,
+ * K = R/ne, a~ = alpha/ne^2):
+ *   P(u,p) = a1~ sum |grad u - p| + a0~ sum |E p|_W* + D(u),  u in [0, U]
+ *   D_KL = (1/ne) sum mu (R u - f + f log(f/R u)),  D_L2 = sum mu/(2 ne^2) |R u - f|^2
+ * Dual from the current (v, w, lambda): v~ = E^T w rescaled by theta into its
+ * ball, dual value -F~*(lambda) + U sum min(0, K^T lambda + grad^T v~).
+ * out: [0] primal, [1] dual, [2] P - D, [3] relative gap (P - D)/|P|;
+ * U = 2 max(u). */
 GT_API int gt_gap(gt_problem *p, double out[4]);
+
+/* gt_gap with the box bound U given (U <= 0: 2 max(u)); out additionally
+ * [4] theta, [5] U, [6] data term, [7] F~*(lambda). */
+GT_API int gt_gap_ex(gt_problem *p, double U, double out[8]);
 
 /* Standalone projectors on device memory in the library's device layout
  * (image [N*N][S], sinogram [nang*nd][S]); for tests and data generation.
