@@ -65,6 +65,14 @@ _SIGS = {
     "gt_time_kernels": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     "gt_normest_noalloc": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P,
                                           ctypes.POINTER(ctypes.c_double)]),
+    "gt_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(GtDesc), ctypes.POINTER(ctypes.c_void_p)]),
+    "gt_batch_destroy": (None, [_P]),
+    "gt_batch_size": (ctypes.c_int, [_P]),
+    "gt_batch_problem": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "gt_batch_run": (ctypes.c_int, [_P, ctypes.c_int]),
+    "gt_batch_synchronize": (ctypes.c_int, [_P]),
+    "gt_batch_invalidate": (ctypes.c_int, [_P]),
+    "gt_batch_set_concurrency": (ctypes.c_int, [_P, ctypes.c_int]),
     "gt_last_error": (ctypes.c_char_p, []),
     "gt_version": (ctypes.c_char_p, []),
 }

@@ -226,7 +226,7 @@ int autotune(gt_problem *p) {
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   // configurations interleaved over several rounds; each keeps its fastest round
-  float ms_cfg[2][8];
+  float ms_cfg[2][16];
   for (auto &r : ms_cfg) for (float &v : r) v = 1e30f;
   int rc = GT_OK;
   const bool log = std::getenv("GRAPTOR_TUNE_LOG") != nullptr;
@@ -684,6 +684,156 @@ int gt_radon(const float *img_dev, float *sino_dev, const double *angles, int N,
 int gt_radon_ad(const float *sino_dev, float *img_dev, const double *angles, int N, int nd, int nang, int S,
                 void *stream) {
   return run_projector(false, sino_dev, img_dev, angles, N, nd, nang, S, stream);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: many independent problems (uneven sizes, channels, angle sets,
+// discrepancies) advanced together.  Each problem keeps its buffers and tuned
+// launch shapes; a chunk of iterations of all problems is captured into one
+// CUDA graph as parallel branches (fork from a batch stream, join back), so one
+// graph launch drives the whole batch and the GPU overlaps the problems' kernels.
+// ---------------------------------------------------------------------------
+struct gt_batch {
+  std::vector<gt_problem *> probs;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t g_chunk = nullptr, g_one = nullptr;
+  int chunk = 8;
+  int chains = 8;  // problems are spread over this many concurrent chains
+  long long iters = 0;
+};
+
+// One iteration of every problem: problem k runs on chain k % chains; chains run
+// concurrently, problems of one chain one after another.
+static int batch_capture(gt_batch *b, int n, cudaGraphExec_t *out) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = GT_OK;
+  cudaError_t e = cudaSuccess;
+  const size_t np = b->probs.size();
+  const size_t chains = std::max<size_t>(1, std::min<size_t>(np, (size_t)b->chains));
+  for (int it = 0; it < n && rc == GT_OK && e == cudaSuccess; ++it) {
+    e = cudaEventRecord(b->fork, b->stream);
+    for (size_t k = 0; k < np && rc == GT_OK && e == cudaSuccess; ++k) {
+      gt_problem *p = b->probs[k];
+      // first problem of a chain waits for the fork, the others for their predecessor
+      e = cudaStreamWaitEvent(p->stream, k < chains ? b->fork : b->joins[k - chains], 0);
+      if (e == cudaSuccess) rc = enqueue_iteration(p);
+      if (rc == GT_OK && e == cudaSuccess) e = cudaEventRecord(b->joins[k], p->stream);
+    }
+    for (size_t k = np - std::min(np, chains); k < np && rc == GT_OK && e == cudaSuccess; ++k)
+      e = cudaStreamWaitEvent(b->stream, b->joins[k], 0);
+  }
+  cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+  if (rc != GT_OK || e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (rc) return rc;
+    return cuda_err(e != cudaSuccess ? e : e2, "batch capture", __LINE__);
+  }
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_err(e, "cudaGraphInstantiate (batch)", __LINE__);
+  return GT_OK;
+}
+
+extern "C" {
+
+void gt_batch_destroy(gt_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->g_chunk) cudaGraphExecDestroy(b->g_chunk);
+  if (b->g_one) cudaGraphExecDestroy(b->g_one);
+  for (auto e : b->joins) if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  for (auto p : b->probs) gt_problem_destroy(p);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int gt_batch_create(int n, const gt_desc *descs, gt_batch **out) {
+  if (!descs || !out || n < 1) return set_err(GT_ERR_ARG, "gt_batch_create: need n >= 1 descriptions");
+  *out = nullptr;
+  for (int k = 1; k < n; ++k)
+    if (descs[k].device != descs[0].device) return set_err(GT_ERR_ARG, "gt_batch_create: one device per batch");
+  gt_batch *b = new (std::nothrow) gt_batch();
+  if (!b) return set_err(GT_ERR_OOM, "host allocation failed");
+  b->device = descs[0].device;
+  cudaError_t e = cudaSetDevice(b->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) { gt_batch_destroy(b); return cuda_err(e, "batch setup", __LINE__); }
+  for (int k = 0; k < n; ++k) {
+    gt_desc d = descs[k];
+    d.stream = nullptr;  // every problem runs on its own stream
+    gt_problem *p = nullptr;
+    const int rc = gt_problem_create(&d, &p);
+    if (rc) { gt_batch_destroy(b); return rc; }
+    b->probs.push_back(p);
+    cudaEvent_t ev = nullptr;
+    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+      gt_batch_destroy(b);
+      return cuda_err(e, "batch events", __LINE__);
+    }
+    b->joins.push_back(ev);
+  }
+  *out = b;
+  return GT_OK;
+}
+
+int gt_batch_size(const gt_batch *b) { return b ? (int)b->probs.size() : 0; }
+
+int gt_batch_problem(gt_batch *b, int k, gt_problem **out) {
+  if (!b || !out || k < 0 || k >= (int)b->probs.size()) return set_err(GT_ERR_ARG, "gt_batch_problem: bad index");
+  *out = b->probs[k];
+  return GT_OK;
+}
+
+int gt_batch_run(gt_batch *b, int iters) {
+  if (!b) return set_err(GT_ERR_ARG, "null batch");
+  if (iters < 0) return set_err(GT_ERR_ARG, "negative iteration count");
+  for (auto p : b->probs)
+    if (!p->has_data) return set_err(GT_ERR_STATE, "gt_batch_run before every problem has data");
+  if (iters == 0) return GT_OK;
+  CK(cudaSetDevice(b->device));
+  // problems' own streams may still carry set-up work: the batch stream waits for it
+  for (size_t k = 0; k < b->probs.size(); ++k) {
+    CK(cudaEventRecord(b->joins[k], b->probs[k]->stream));
+    CK(cudaStreamWaitEvent(b->stream, b->joins[k], 0));
+  }
+  int rc;
+  if (iters >= b->chunk && !b->g_chunk && (rc = batch_capture(b, b->chunk, &b->g_chunk)) != GT_OK) return rc;
+  if (!b->g_one && (rc = batch_capture(b, 1, &b->g_one)) != GT_OK) return rc;
+  int left = iters;
+  while (left >= b->chunk) { CK(cudaGraphLaunch(b->g_chunk, b->stream)); left -= b->chunk; }
+  while (left > 0) { CK(cudaGraphLaunch(b->g_one, b->stream)); --left; }
+  for (auto p : b->probs) p->iters += iters;
+  b->iters += iters;
+  return GT_OK;
+}
+
+int gt_batch_synchronize(gt_batch *b) {
+  if (!b) return set_err(GT_ERR_ARG, "null batch");
+  CK(cudaSetDevice(b->device));
+  CK(cudaStreamSynchronize(b->stream));
+  return GT_OK;
+}
+
+int gt_batch_set_concurrency(gt_batch *b, int chains) {
+  if (!b || chains < 1) return set_err(GT_ERR_ARG, "gt_batch_set_concurrency: chains must be >= 1");
+  b->chains = chains;
+  return gt_batch_invalidate(b);
+}
+
+int gt_batch_invalidate(gt_batch *b) {
+  if (!b) return set_err(GT_ERR_ARG, "null batch");
+  if (b->g_chunk) { cudaGraphExecDestroy(b->g_chunk); b->g_chunk = nullptr; }
+  if (b->g_one) { cudaGraphExecDestroy(b->g_one); b->g_one = nullptr; }
+  return GT_OK;
 }
 
 }  // extern "C"

@@ -1415,7 +1415,13 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // (8, 4, table), (4, 2, table), (4, 4, table), (8, 1, on the fly), (4, 1, on the fly),
 // (8, 2, on the fly), (4, 2, on the fly).
 // Otherwise one fixed shape with 2 or 1 slices per thread.
-int num_proj_configs(int S, int which) { return S % 4 == 0 ? (which == 0 ? 4 : 8) : 1; }
+// For S a multiple of 4 up to 64, one more candidate each: one slice per thread
+// (k_fwd config 4, k_bp config 8), which keeps all lanes busy when S is small.
+int num_proj_configs(int S, int which) {
+  if (S % 4 != 0) return 1;
+  const int extra = S <= 64 ? 1 : 0;
+  return (which == 0 ? 4 : 8) + extra;
+}
 
 template <int VW, int UNR>
 static void fwd_vw(const IterParams &P, int disc, cudaStream_t st) {
@@ -1431,6 +1437,7 @@ cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
       case 1: fwd_vw<8, 8>(P, disc, st); break;
       case 2: fwd_vw<4, 4>(P, disc, st); break;
       case 3: fwd_vw<4, 8>(P, disc, st); break;
+      case 4: fwd_vw<1, 4>(P, disc, st); break;
       default: fwd_vw<8, 4>(P, disc, st); break;
     }
   } else if (S % 2 == 0) {
@@ -1457,6 +1464,7 @@ cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
       case 5: bp_vw<4, 1, false>(P, st); break;
       case 6: bp_vw<8, 2, false>(P, st); break;
       case 7: bp_vw<4, 2, false>(P, st); break;
+      case 8: bp_vw<1, 1, false>(P, st); break;
       default: bp_vw<8, 2>(P, st); break;
     }
   } else if (S % 2 == 0) {

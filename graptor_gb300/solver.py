@@ -40,8 +40,9 @@ class Problem:
 
     def __init__(self, dim, N, Nz, C, nd, angles, alpha=(4.0, 1.0), mu=None, discrepancy="KL",
                  regularisation="TGV", coupling="FROB", stepsize=1.0, normest=None, device=0, stream=None,
-                 autotune=True):
+                 autotune=True, _handle=None):
         self._h = None
+        self._owner = _handle is None
         self.dim, self.N, self.Nz, self.C, self.nd = int(dim), int(N), int(Nz), int(C), int(nd)
         self.angles = np.ascontiguousarray(angles, dtype=np.float64)
         self.nang = int(self.angles.size)
@@ -51,30 +52,41 @@ class Problem:
         alpha = np.atleast_1d(np.asarray(alpha, dtype=np.float64))
         if alpha.size == 1:
             alpha = np.array([alpha[0], alpha[0]])
+        self.alpha = alpha
         self.mu = np.ascontiguousarray(np.ones(self.C) if mu is None else mu, dtype=np.float64)
         if self.mu.size != self.C:
             raise ValueError(f"mu has {self.mu.size} entries for {self.C} channels")
         self.regularisation = regularisation.upper()
+        self.discrepancy, self.coupling = discrepancy.upper(), coupling.upper()
+        self.stepsize, self.normest_in, self.device = float(stepsize), normest, int(device)
+        self._stream, self._autotune = stream, bool(autotune)
+        if _handle is not None:
+            self._h = _handle
+            return
+        h = ctypes.c_void_p()
+        L.check(L.lib().gt_problem_create(ctypes.byref(self.desc()), ctypes.byref(h)))
+        self._h = h
+
+    def desc(self) -> L.GtDesc:
+        """The C description of this problem (arrays stay owned by self)."""
         d = L.GtDesc()
         d.dim, d.N, d.Nz, d.C, d.nd, d.nang = self.dim, self.N, self.Nz, self.C, self.nd, self.nang
         d.angles = self.angles.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-        d.stepsize = float(stepsize)
-        d.alpha0, d.alpha1 = float(alpha[0]), float(alpha[1])
+        d.stepsize = self.stepsize
+        d.alpha0, d.alpha1 = float(self.alpha[0]), float(self.alpha[1])
         d.mu = self.mu.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-        d.discrepancy = DISCREPANCY[discrepancy.upper()]
+        d.discrepancy = DISCREPANCY[self.discrepancy]
         d.regularisation = REGULARISATION[self.regularisation]
-        d.coupling = COUPLING[coupling.upper()]
-        d.normest = float(normest) if normest else 0.0
-        d.device = int(device)
-        d.stream = stream
-        d.autotune = int(bool(autotune))
-        h = ctypes.c_void_p()
-        L.check(L.lib().gt_problem_create(ctypes.byref(d), ctypes.byref(h)))
-        self._h = h
+        d.coupling = COUPLING[self.coupling]
+        d.normest = float(self.normest_in) if self.normest_in else 0.0
+        d.device = self.device
+        d.stream = self._stream
+        d.autotune = int(self._autotune)
+        return d
 
     # ------------------------------------------------------------------ lifecycle
     def close(self):
-        if self._h is not None and self._h.value:
+        if self._owner and self._h is not None and self._h.value:
             L.lib().gt_problem_destroy(self._h)
         self._h = None
 
@@ -160,6 +172,67 @@ class Problem:
     @property
     def launches_per_iteration(self) -> int:
         return int(L.lib().gt_launches_per_iteration(self._h))
+
+
+class Batch:
+    """Independent problems advanced together by one graph launch per chunk.
+
+    ``specs`` are keyword dicts of :class:`Problem` (dim, N, Nz, C, nd, angles, ...).
+    Members are :class:`Problem` views (``batch[k]``) for data and results; the
+    batch owns them."""
+
+    def __init__(self, specs, device=0):
+        self._b = None
+        self._views = [Problem(**{**sp, "device": device}, _handle=ctypes.c_void_p(0)) for sp in specs]
+        descs = (L.GtDesc * len(self._views))(*[v.desc() for v in self._views])
+        b = ctypes.c_void_p()
+        L.check(L.lib().gt_batch_create(len(self._views), descs, ctypes.byref(b)))
+        self._b = b
+        for k, v in enumerate(self._views):
+            h = ctypes.c_void_p()
+            L.check(L.lib().gt_batch_problem(self._b, k, ctypes.byref(h)))
+            v._h = h
+
+    def __len__(self):
+        return len(self._views)
+
+    def __getitem__(self, k) -> Problem:
+        return self._views[k]
+
+    def run(self, iters: int):
+        L.check(L.lib().gt_batch_run(self._b, int(iters)))
+        return self
+
+    def synchronize(self):
+        L.check(L.lib().gt_batch_synchronize(self._b))
+        return self
+
+    def invalidate(self):
+        L.check(L.lib().gt_batch_invalidate(self._b))
+
+    def set_concurrency(self, chains: int):
+        """Spread the problems over `chains` concurrent chains (default 8)."""
+        L.check(L.lib().gt_batch_set_concurrency(self._b, int(chains)))
+        return self
+
+    def close(self):
+        if self._b is not None and self._b.value:
+            for v in self._views:
+                v._h = None
+            L.lib().gt_batch_destroy(self._b)
+        self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def radon(img_dev, sino_dev, angles, N, nd, S, stream=None):

@@ -151,6 +151,26 @@ GT_API int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n);
  * for that device: make it before any stream capture. */
 GT_API int gt_normest_noalloc(const double *angles, int N, int nd, int nang, int device, void *stream, double *out);
 
+/* Batches of independent problems (uneven sizes, channels, angle sets,
+ * discrepancies) on one device.  Each problem keeps its own buffers and tuned
+ * launch shapes; gt_batch_run captures a chunk of iterations of all problems
+ * into one CUDA graph as parallel branches and launches it, so one launch
+ * advances the whole batch.  Data and results go through the member problems
+ * (gt_batch_problem + gt_set_data / gt_get_state / gt_gap).  After changing a
+ * member's data call gt_batch_invalidate before the next gt_batch_run.
+ * (The reference solves problems one at a time: Reconstruction_coupled.py:188, :414.) */
+typedef struct gt_batch gt_batch;
+GT_API int gt_batch_create(int n, const gt_desc *descs, gt_batch **out);
+GT_API void gt_batch_destroy(gt_batch *b);
+GT_API int gt_batch_size(const gt_batch *b);
+GT_API int gt_batch_problem(gt_batch *b, int k, gt_problem **out);
+GT_API int gt_batch_run(gt_batch *b, int iters);
+GT_API int gt_batch_synchronize(gt_batch *b);
+GT_API int gt_batch_invalidate(gt_batch *b);
+/* Run the batch's problems on `chains` concurrent chains (problem k on chain
+ * k mod chains, one after another within a chain); default 8. */
+GT_API int gt_batch_set_concurrency(gt_batch *b, int chains);
+
 /* Number of kernel launches one iteration issues (for launch accounting). */
 GT_API int gt_launches_per_iteration(const gt_problem *p);
 

@@ -227,3 +227,27 @@ def test_fp64_normest_matches_reference_estimate(golden):
         ne = p.scalars["normest"]
         p.close()
         assert abs(ne - float(g["normest"])) / float(g["normest"]) < 1e-4, (name, ne, float(g["normest"]))
+
+
+def test_batch_matches_individual_problems():
+    """A batch of uneven problems (sizes, channels, angle sets, KL/L2, 2-D/3-D)
+    gives each member the result it gets when solved alone."""
+    from graptor_gb300 import phantom
+    from graptor_gb300.solver import Batch, Problem
+    rng = np.random.default_rng(11)
+    specs, datas = [], []
+    for k, (dim, N, Nz, C, nang, disc) in enumerate([(3, 24, 5, 2, 20, "KL"), (3, 17, 3, 1, 13, "L2"),
+                                                     (2, 30, 4, 3, 25, "KL"), (3, 20, 6, 4, 30, "L2")]):
+        ang = phantom.angles_deg(nang, -75, 75)
+        specs.append(dict(dim=dim, N=N, Nz=Nz, C=C, nd=N, angles=ang, alpha=(4.0, 1.0), mu=rng.uniform(0.1, 0.4, C),
+                          discrepancy=disc, regularisation="TGV", coupling="FROB", normest=12.0 + k))
+        datas.append(np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32))
+    with Batch(specs) as b:
+        for k in range(len(b)):
+            b[k].set_data(datas[k])
+        b.run(37).synchronize()
+        got = [b[k].get("u") for k in range(len(b))]
+    for k, sp in enumerate(specs):
+        with Problem(**sp) as p:
+            p.set_data(datas[k]).run(37).synchronize()
+            np.testing.assert_array_equal(got[k], p.get("u"), err_msg=f"member {k}")
