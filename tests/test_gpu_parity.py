@@ -251,3 +251,16 @@ def test_batch_matches_individual_problems():
         with Problem(**sp) as p:
             p.set_data(datas[k]).run(37).synchronize()
             np.testing.assert_array_equal(got[k], p.get("u"), err_msg=f"member {k}")
+
+
+def test_out_of_memory_is_a_memory_error():
+    """An allocation the device cannot hold fails cleanly as GraptorMemoryError (the
+    reference's pyopencl.MemoryError, which Reconstruction_coupled.py:509-536
+    answers by shrinking the slice chunk); the device stays usable."""
+    from graptor_gb300 import GraptorMemoryError, phantom
+    from graptor_gb300.solver import Problem
+    ang = phantom.angles_deg(30)
+    with pytest.raises(GraptorMemoryError):
+        Problem(3, 4096, 256, 8, 4096, ang, (4, 1), np.ones(8))   # ~18 TB of state
+    with Problem(3, 16, 2, 1, 16, ang, (4, 1), [0.2], normest=10.0) as p:  # still usable
+        p.set_data(np.ones((2, 30, 16), np.float32)).run(2).synchronize()
