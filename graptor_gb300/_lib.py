@@ -47,6 +47,8 @@ class GtDesc(ctypes.Structure):
 
 
 _P = ctypes.c_void_p
+_I = ctypes.c_int
+_LL = ctypes.c_longlong
 _SIGS = {
     "gt_problem_create": (ctypes.c_int, [ctypes.POINTER(GtDesc), ctypes.POINTER(ctypes.c_void_p)]),
     "gt_problem_destroy": (None, [_P]),
@@ -73,6 +75,26 @@ _SIGS = {
     "gt_batch_synchronize": (ctypes.c_int, [_P]),
     "gt_batch_invalidate": (ctypes.c_int, [_P]),
     "gt_batch_set_concurrency": (ctypes.c_int, [_P, ctypes.c_int]),
+    "gt_get_state_device": (ctypes.c_int, [_P, ctypes.c_int, _P]),
+    "gt_set_state_device": (ctypes.c_int, [_P, ctypes.c_int, _P]),
+    "gt_problem_stream": (ctypes.c_void_p, [_P]),
+    "gt_dual_from_primal": (ctypes.c_int, [_P]),
+    "gt_set_tuning": (ctypes.c_int, [_P, _I, _I]),
+    "gt_nn_conv3d": (ctypes.c_int, [_P, _I, _I, _I, _I, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P]),
+    "gt_nn_flip_weights": (ctypes.c_int, [_P, _P, _I, _I, _I, _P]),
+    "gt_nn_conv3d_wgrad": (ctypes.c_int, [_P, _I, _I, _I, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _LL, _P, _P, _I,
+                                          _P]),
+    "gt_nn_bias_grad": (ctypes.c_int, [_P, _I, _I, _I, _I, _LL, _P, _I, _P]),
+    "gt_nn_scale": (ctypes.c_int, [_P, _I, _P, _I, _I, _I, _LL, _P, _I, _P]),
+    "gt_nn_relu_bwd": (ctypes.c_int, [_P, _P, _I, _I, _I, _I, _I, _LL, _P]),
+    "gt_nn_pool2": (ctypes.c_int, [_P, _I, _I, _P, _I, _I, _I, _I, _I, _P]),
+    "gt_nn_pool2_bwd": (ctypes.c_int, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _P]),
+    "gt_nn_up2": (ctypes.c_int, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _P]),
+    "gt_nn_up2_bwd": (ctypes.c_int, [_P, _I, _I, _P, _I, _I, _I, _I, _I, _P]),
+    "gt_nn_mse": (ctypes.c_int, [_P, _P, _LL, _P, _P, _P]),
+    "gt_nn_adam": (ctypes.c_int, [_P, _P, _P, _P, _P, _LL, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, _I, _P]),
+    "gt_nn_cast": (ctypes.c_int, [_P, _I, _P, _LL, _P]),
     "gt_last_error": (ctypes.c_char_p, []),
     "gt_version": (ctypes.c_char_p, []),
 }

@@ -30,6 +30,8 @@ cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, in
                             cudaStream_t st);
 cudaError_t launch_transpose(const float *in, float *out, int rows, int cols, cudaStream_t st);
 cudaError_t launch_feasible(float *f, const float *r1, int nbin1, int S, cudaStream_t st);
+cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
+                                int Nz, int disc, cudaStream_t st);
 cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, double *d_img, double *d_sino,
                       double *d_part, double *out, cudaStream_t st);
 cudaError_t fill_f64(double *x, size_t n, double v, cudaStream_t st);
@@ -559,6 +561,63 @@ int gt_set_state(gt_problem *p, int field, const float *host) {
     CK(gt::launch_transpose(p->stage, ptr + k * plane, (int)S, (int)X, p->stream));
   }
   CK(cudaStreamSynchronize(p->stream));
+  return GT_OK;
+}
+
+int gt_get_state_device(gt_problem *p, int field, float *dev) {
+  if (!p || !dev) return set_err(GT_ERR_ARG, "null argument");
+  float *ptr; int comps; size_t X;
+  int rc = field_info(p, field, &ptr, &comps, &X);
+  if (rc) return rc;
+  CK(cudaSetDevice(p->device));
+  const size_t S = p->d.S;
+  for (int k = 0; k < comps; ++k) {
+    const size_t plane = (field == GT_LAMBDA || field == GT_KU || field == GT_DATA) ? p->d.nbin : p->d.vol;
+    CK(gt::launch_transpose(ptr + k * plane, dev + k * X * S, (int)X, (int)S, p->stream));
+  }
+  return GT_OK;
+}
+
+int gt_set_state_device(gt_problem *p, int field, const float *dev) {
+  if (!p || !dev) return set_err(GT_ERR_ARG, "null argument");
+  float *ptr; int comps; size_t X;
+  int rc = field_info(p, field, &ptr, &comps, &X);
+  if (rc) return rc;
+  CK(cudaSetDevice(p->device));
+  const size_t S = p->d.S;
+  for (int k = 0; k < comps; ++k) {
+    const size_t plane = (field == GT_LAMBDA || field == GT_KU || field == GT_DATA) ? p->d.nbin : p->d.vol;
+    CK(gt::launch_transpose(dev + k * X * S, ptr + k * plane, (int)S, (int)X, p->stream));
+  }
+  return GT_OK;
+}
+
+int gt_dual_from_primal(gt_problem *p) {
+  if (!p) return set_err(GT_ERR_ARG, "null argument");
+  if (!p->has_data) return set_err(GT_ERR_STATE, "gt_dual_from_primal before gt_set_data");
+  CK(cudaSetDevice(p->device));
+  // K u into the ku buffer (the next iteration's forward projection overwrites it)
+  CK(gt::launch_radon(p->u, p->ku, p->ofs, p->d.N, p->d.nd, p->d.nang, p->d.S, p->stream));
+  CK(gt::launch_lambda_fixed(p->lam, p->ku, p->f, p->mu64, (long long)p->d.nd * p->d.nang, p->d.S, p->d.Nz, p->disc,
+                             p->stream));
+  return GT_OK;
+}
+
+void *gt_problem_stream(gt_problem *p) { return p ? (void *)p->stream : nullptr; }
+
+int gt_set_tuning(gt_problem *p, int fwd_cfg, int bp_cfg) {
+  if (!p) return set_err(GT_ERR_ARG, "null argument");
+  if (fwd_cfg < 0 || fwd_cfg >= gt::num_proj_configs(p->d.S, 0) || bp_cfg < 0 ||
+      bp_cfg >= gt::num_proj_configs(p->d.S, 1))
+    return set_err(GT_ERR_ARG, "launch configuration out of range (%d forward, %d back-projection configurations)",
+                   gt::num_proj_configs(p->d.S, 0), gt::num_proj_configs(p->d.S, 1));
+  CK(cudaSetDevice(p->device));
+  CK(cudaStreamSynchronize(p->stream));
+  p->P.fwd_cfg = fwd_cfg;
+  p->P.bp_cfg = bp_cfg;
+  // the captured graphs hold the old launch shapes
+  if (p->g_one) { cudaGraphExecDestroy(p->g_one); p->g_one = nullptr; }
+  if (p->g_chunk) { cudaGraphExecDestroy(p->g_chunk); p->g_chunk = nullptr; }
   return GT_OK;
 }
 

@@ -1061,6 +1061,30 @@ __global__ void k_feasible(float *__restrict__ f, const float *__restrict__ r1, 
   if (r1[t / S] <= 0.f) f[t] = 0.f;
 }
 
+// Data dual consistent with a primal image: lambda at the fixed point of the
+// lambda update for the given K u.  KL (update_lambda_KL, 3-D :690-704): the
+// fixed point of lam = s - (s - mu + sqrt((s - mu)^2 + 4 sigma f mu)) / 2 with
+// s = lam + sigma ku is lam = mu (1 - f / ku); where ku <= 0 lambda is kept.
+// L2 (update_lambda_L2, :677-688, weight m = mu / (sigma + mu)): lam = mu (ku - f).
+__global__ void k_lambda_fixed(float *__restrict__ lam, const float *__restrict__ ku, const float *__restrict__ f,
+                               const double *__restrict__ mu, long long nbin, int S, int Nz, int disc) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nbin * S) return;
+  const int s = (int)(t % S);
+  const float m = (float)mu[s / Nz], k = ku[t], fv = f[t];
+  if (disc == 0) {
+    if (k > 0.f) lam[t] = m * (1.0f - fv / k);
+  } else {
+    lam[t] = m * (k - fv);
+  }
+}
+
+cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
+                                int Nz, int disc, cudaStream_t st) {
+  k_lambda_fixed<<<(unsigned)((nbin * S + 255) / 256), 256, 0, st>>>(lam, ku, f, mu, nbin, S, Nz, disc);
+  return cudaGetLastError();
+}
+
 template <class T>
 __global__ void k_fill(T *__restrict__ x, size_t n, T v) {
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) x[k] = v;
@@ -1405,12 +1429,113 @@ cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st) 
   return tgv ? launch_dual_t<2, true>(P, cpl, st) : launch_dual_t<2, false>(P, cpl, st);
 }
 
+// Forward projection of R adjacent bins of one angle at once.  For every row the
+// union of the R bins' x ranges is read once and each pixel feeds every bin whose
+// hat covers it, so a pixel loaded for bin i also serves bin i+1 (about (R+1)/2R
+// of the loads of one bin at a time).  Each bin still sums its terms in the
+// reference's order (rows ascending, x ascending) with the reference's bounds and
+// weights.
+template <int VW, int R, bool EXACT>
+__device__ __forceinline__ void radon_run(const float *__restrict__ img, size_t S, int N, int nd, const float4 o,
+                                          int i0, const Slices<VW> &sl, float (&acc)[R][VW]) {
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int k = 0; k < VW; ++k) acc[r][k] = 0.f;
+  int ylo, yhi, ylo2, yhi2;
+  ray_rows(o, i0, N, ylo, yhi);
+  ray_rows(o, min(i0 + R - 1, nd - 1), N, ylo2, yhi2);
+  ylo = min(ylo, ylo2);
+  yhi = max(yhi, yhi2);
+  for (int y = ylo; y <= yhi; ++y) {
+    const float d = __fadd_rn(__fmul_rn((float)y, o.y), o.z);
+    int xl[R], xh[R];
+    int xmin = N, xmax = -1;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int i = i0 + r;
+      const float fim = (float)(i - 1), fip = (float)(i + 1);
+      int a, b;
+      if (o.x == 0.f) {
+        if (d > fim && d < fip) { a = 0; b = N - 1; } else { a = N; b = -1; }
+      } else if (o.x > 0.f) {
+        a = __float2int_rz(__fmul_rn(__fsub_rn(fim, d), o.w));
+        b = __float2int_rz(__fmul_rn(__fsub_rn(fip, d), o.w));
+      } else {
+        a = __float2int_rz(__fmul_rn(__fsub_rn(fip, d), o.w));
+        b = __float2int_rz(__fmul_rn(__fsub_rn(fim, d), o.w));
+      }
+      a = max(a, 0);
+      b = min(b, N - 1);
+      if (i >= nd) { a = N; b = -1; }
+      xl[r] = a;
+      xh[r] = b;
+      if (a <= b) { xmin = min(xmin, a); xmax = max(xmax, b); }
+    }
+    const float *row = img + (size_t)y * N * S;
+#pragma unroll 2
+    for (int x = xmin; x <= xmax; ++x) {
+      float val[VW];
+      sl.load(row + (size_t)x * S, val);
+      const float tx = __fadd_rn(__fmul_rn((float)x, o.x), d);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float wgt = 1.0f - fabsf(__fsub_rn(tx, (float)(i0 + r)));
+        if (x >= xl[r] && x <= xh[r] && wgt > 0.f) {
+#pragma unroll
+          for (int k = 0; k < VW; ++k) acc[r][k] = mac<EXACT>(acc[r][k], wgt, val[k]);
+        }
+      }
+    }
+  }
+}
+
+// k_fwd_run: k_fwd for runs of R bins (radon_run), same fused data-term prox.
+template <int DISC, int VW, int R>
+__global__ void __launch_bounds__(256) k_fwd_run(const IterParams P) {
+  const Dims d = P.d;
+  const int nrun = (d.nd + R - 1) / R;
+  long long unit;
+  Slices<VW> sl;
+  if (!map_thread<VW>((long long)nrun * d.nang, d.S, unit, sl)) return;
+  const int j = (int)(unit / nrun), i0 = (int)(unit - (long long)j * nrun) * R;
+  float acc[R][VW];
+  radon_run<VW, R, false>(P.ubar, d.S, d.N, d.nd, __ldg(P.ofs + j), i0, sl, acc);
+  const float sd = P.sigma_data;
+  float m[VW];
+#pragma unroll
+  for (int k = 0; k < VW; ++k) m[k] = sl.valid(k) ? __ldg(P.mu + sl.slice(k) / d.Nz) : 0.f;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    if (i0 + r >= d.nd) break;
+    const size_t q = ((size_t)j * d.nd + i0 + r) * d.S;
+    sl.store(P.ku + q, acc[r]);
+    float lam[VW], f[VW];
+    sl.loadw(P.lam + q, lam);
+    sl.load(P.f + q, f);
+#pragma unroll
+    for (int k = 0; k < VW; ++k) {
+      if (DISC == KL) {
+        const float sv = lam[k] + sd * acc[r][k];
+        const float wv = sv - m[k];
+        const float dv = wv * wv + 4.f * sd * f[k] * m[k];
+        lam[k] = sv - 0.5f * (wv + sqrtf(dv));
+      } else {
+        lam[k] = (lam[k] + sd * (acc[r][k] - f[k])) * m[k];
+      }
+    }
+    sl.store(P.lam + q, lam);
+  }
+}
+
 // slices per lane: 8 (two float4 chunks) when S is a multiple of 4, else 2, else 1
 static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 : 1); }
 
 // Tunable launch shapes of the projector kernels (chosen per problem shape by
 // the autotuner in gt_api.cu).  S a multiple of 4: k_fwd configs 0..3 =
-// (slices per lane, ray-table entries in flight) = (8, 4), (8, 8), (4, 4), (4, 8);
+// (slices per lane, ray-table entries in flight) = (8, 4), (8, 8), (4, 4), (4, 8),
+// configs 5..8 = (slices per lane, bins per run) of k_fwd_run = (8, 2), (8, 4),
+// (4, 4), (4, 8);
 // k_bp configs 0..7 = (slices per lane, angles per step, geometry) = (8, 2, table),
 // (8, 4, table), (4, 2, table), (4, 4, table), (8, 1, on the fly), (4, 1, on the fly),
 // (8, 2, on the fly), (4, 2, on the fly).
@@ -1419,8 +1544,8 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // (k_fwd config 4, k_bp config 8), which keeps all lanes busy when S is small.
 int num_proj_configs(int S, int which) {
   if (S % 4 != 0) return 1;
-  const int extra = S <= 64 ? 1 : 0;
-  return (which == 0 ? 4 : 8) + extra;
+  if (which == 0) return 9;  // config 4 (one slice per thread) is kept as a candidate for every S
+  return S <= 64 ? 9 : 8;
 }
 
 template <int VW, int UNR>
@@ -1428,6 +1553,14 @@ static void fwd_vw(const IterParams &P, int disc, cudaStream_t st) {
   const unsigned g = blocks_for(threads_for<VW>((long long)P.d.nd * P.d.nang, P.d.S), 256);
   if (disc == KL) k_fwd<KL, VW, UNR><<<g, 256, 0, st>>>(P);
   else k_fwd<L2, VW, UNR><<<g, 256, 0, st>>>(P);
+}
+
+template <int VW, int R>
+static void fwd_run(const IterParams &P, int disc, cudaStream_t st) {
+  const long long units = (long long)((P.d.nd + R - 1) / R) * P.d.nang;
+  const unsigned g = blocks_for(threads_for<VW>(units, P.d.S), 256);
+  if (disc == KL) k_fwd_run<KL, VW, R><<<g, 256, 0, st>>>(P);
+  else k_fwd_run<L2, VW, R><<<g, 256, 0, st>>>(P);
 }
 
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
@@ -1438,6 +1571,10 @@ cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
       case 2: fwd_vw<4, 4>(P, disc, st); break;
       case 3: fwd_vw<4, 8>(P, disc, st); break;
       case 4: fwd_vw<1, 4>(P, disc, st); break;
+      case 5: fwd_run<8, 2>(P, disc, st); break;
+      case 6: fwd_run<8, 4>(P, disc, st); break;
+      case 7: fwd_run<4, 4>(P, disc, st); break;
+      case 8: fwd_run<4, 8>(P, disc, st); break;
       default: fwd_vw<8, 4>(P, disc, st); break;
     }
   } else if (S % 2 == 0) {

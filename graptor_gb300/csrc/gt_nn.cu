@@ -1,0 +1,542 @@
+// Kernels of the warm-start network: a small 3-D U-Net trained and run with
+// BF16 weights and activations and FP32 accumulation.  No counterpart in the
+// reference (it has no learned component).
+//
+// Tensors are [B][C][D][H][W] (W fastest).  Convolutions are 3x3x3 or 1x1x1,
+// stride 1, zero padding (k-1)/2.  Outputs can be written at a channel offset of
+// a wider tensor (the U-Net's skip concatenation is free) and can accumulate.
+//
+//   gt_nn_conv3d        forward (and, with transformed weights, the data gradient)
+//   gt_nn_flip_weights  w[co][ci][t] -> w'[ci][co][K3-1-t]   (data-gradient weights)
+//   gt_nn_conv3d_wgrad  weight gradient as a split-K GEMM  dW = dY * im2col(X)^T
+//   gt_nn_bias_grad, gt_nn_relu_bwd, gt_nn_pool2 / _bwd, gt_nn_up2 / _bwd,
+//   gt_nn_mse, gt_nn_adam, gt_nn_cast
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "graptor_gb300.h"
+
+namespace {
+
+template <class T> __device__ __forceinline__ float ld(const T *p) { return (float)*p; }
+template <> __device__ __forceinline__ float ld<__nv_bfloat16>(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+template <class T> __device__ __forceinline__ void st(T *p, float v) { *p = (T)v; }
+template <> __device__ __forceinline__ void st<__nv_bfloat16>(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
+
+struct Shape {
+  int B, D, H, W;
+};
+
+// ---------------------------------------------------------------------------
+// forward convolution: a thread computes CO_T output channels for VX voxels
+// along W; the block stages the weights of its channel tile, CI_CH input
+// channels at a time, in shared memory (converted to FP32).
+// ---------------------------------------------------------------------------
+constexpr int CI_CH = 8;
+
+template <class TI, class TO, int KS, int CO_T, int VX>
+__global__ void __launch_bounds__(128) k_conv3d(const TI *__restrict__ x, int Ci, int Cx, int x_off,
+                                                const __nv_bfloat16 *__restrict__ w,
+                                                const float *__restrict__ bias, TO *__restrict__ y, int Co, int Cy,
+                                                int co_off, Shape s, int relu, int accumulate) {
+  constexpr int K3 = KS * KS * KS, R = KS / 2;
+  __shared__ float sw[CO_T * CI_CH * K3];
+  const int co0 = blockIdx.y * CO_T;
+  const long long nvox = (long long)s.B * s.D * s.H * (s.W / VX);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = t < nvox;
+  int b = 0, d = 0, h = 0, w0 = 0;
+  if (active) {
+    long long r = t;
+    const int wq = (int)(r % (s.W / VX)); r /= (s.W / VX);
+    h = (int)(r % s.H); r /= s.H;
+    d = (int)(r % s.D); b = (int)(r / s.D);
+    w0 = wq * VX;
+  }
+  const size_t plane = (size_t)s.H * s.W, vol = plane * s.D;
+  float acc[CO_T][VX];
+#pragma unroll
+  for (int c = 0; c < CO_T; ++c) {
+    const float bv = (bias && co0 + c < Co) ? bias[co0 + c] : 0.f;
+#pragma unroll
+    for (int v = 0; v < VX; ++v) acc[c][v] = bv;
+  }
+  for (int ci0 = 0; ci0 < Ci; ci0 += CI_CH) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < CO_T * CI_CH * K3; k += blockDim.x) {
+      const int c = k / (CI_CH * K3), rem = k - c * CI_CH * K3, ci = rem / K3, tp = rem - ci * K3;
+      sw[k] = (co0 + c < Co && ci0 + ci < Ci) ? __bfloat162float(w[((size_t)(co0 + c) * Ci + ci0 + ci) * K3 + tp]) : 0.f;
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int cmax = min(CI_CH, Ci - ci0);
+    for (int ci = 0; ci < cmax; ++ci) {
+      const TI *xc = x + ((size_t)b * Cx + x_off + ci0 + ci) * vol;
+#pragma unroll
+      for (int kd = 0; kd < KS; ++kd) {
+        const int dd = d + kd - R;
+        if (dd < 0 || dd >= s.D) continue;
+#pragma unroll
+        for (int kh = 0; kh < KS; ++kh) {
+          const int hh = h + kh - R;
+          if (hh < 0 || hh >= s.H) continue;
+          const TI *row = xc + (size_t)dd * plane + (size_t)hh * s.W;
+          float xv[VX + KS - 1];
+#pragma unroll
+          for (int q = 0; q < VX + KS - 1; ++q) {
+            const int ww = w0 + q - R;
+            xv[q] = (ww >= 0 && ww < s.W) ? ld<TI>(row + ww) : 0.f;
+          }
+#pragma unroll
+          for (int kw = 0; kw < KS; ++kw) {
+            const int tp = (kd * KS + kh) * KS + kw;
+#pragma unroll
+            for (int c = 0; c < CO_T; ++c) {
+              const float wv = sw[(c * CI_CH + ci) * K3 + tp];
+#pragma unroll
+              for (int v = 0; v < VX; ++v) acc[c][v] = fmaf(wv, xv[v + kw], acc[c][v]);
+            }
+          }
+        }
+      }
+    }
+  }
+  if (!active) return;
+#pragma unroll
+  for (int c = 0; c < CO_T; ++c) {
+    if (co0 + c >= Co) break;
+    TO *yo = y + ((size_t)b * Cy + co_off + co0 + c) * vol + (size_t)d * plane + (size_t)h * s.W + w0;
+#pragma unroll
+    for (int v = 0; v < VX; ++v) {
+      float r = acc[c][v];
+      if (accumulate) r += ld<TO>(yo + v);
+      if (relu) r = fmaxf(r, 0.f);
+      st<TO>(yo + v, r);
+    }
+  }
+}
+
+// w[co][ci][t] -> w'[ci][co][K3-1-t]: convolving dY with w' gives dX (stride 1, same padding)
+__global__ void k_flip(const __nv_bfloat16 *__restrict__ w, __nv_bfloat16 *__restrict__ wf, int Co, int Ci, int K3) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)Co * Ci * K3) return;
+  const int tp = (int)(t % K3);
+  const long long r = t / K3;
+  const int ci = (int)(r % Ci), co = (int)(r / Ci);
+  wf[((size_t)ci * Co + co) * K3 + (K3 - 1 - tp)] = w[t];
+}
+
+// ---------------------------------------------------------------------------
+// weight gradient: dW[co][ci*K3 + t] = sum_{b, voxel} dY[b][co][v] X[b][ci][v + off(t)]
+// GEMM M = Co, N = Ci*K3, K = voxels; a block computes a 16 x 64 tile over one
+// K-chunk and writes it to part[chunk]; k_wgrad_reduce sums the chunks in order.
+// ---------------------------------------------------------------------------
+constexpr int WG_M = 16, WG_N = 64, WG_K = 32;
+
+template <class TX, int KS>
+__global__ void __launch_bounds__(256) k_wgrad(const float *__restrict__ dy, int Co, int Cdy, int dy_off,
+                                               const TX *__restrict__ x, int Ci, int Cx, int x_off, Shape s,
+                                               long long kchunk, float *__restrict__ part) {
+  constexpr int K3 = KS * KS * KS, R = KS / 2;
+  __shared__ float sa[WG_M][WG_K + 1];
+  __shared__ float sb[WG_K][WG_N + 1];
+  const int m0 = blockIdx.y * WG_M, n0 = blockIdx.x * WG_N, N = Ci * K3;
+  const long long nvox = (long long)s.B * s.D * s.H * s.W;
+  const long long k0 = (long long)blockIdx.z * kchunk, k1 = min(nvox, k0 + kchunk);
+  const size_t plane = (size_t)s.H * s.W, vol = plane * s.D;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 16 x 16 threads, 4 columns each
+  float acc[4] = {0, 0, 0, 0};
+  for (long long kb = k0; kb < k1; kb += WG_K) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < WG_M * WG_K; q += blockDim.x) {
+      const int m = q / WG_K, kk = q - m * WG_K;
+      const long long v = kb + kk;
+      float val = 0.f;
+      if (m0 + m < Co && v < k1) {
+        const long long bb = v / vol, rv = v - bb * vol;
+        val = dy[((size_t)bb * Cdy + dy_off + m0 + m) * vol + rv];
+      }
+      sa[m][kk] = val;
+    }
+    for (int q = threadIdx.x; q < WG_K * WG_N; q += blockDim.x) {
+      const int kk = q / WG_N, n = q - kk * WG_N;
+      const long long v = kb + kk;
+      float val = 0.f;
+      if (n0 + n < N && v < k1) {
+        const int ci = (n0 + n) / K3, tp = (n0 + n) - ci * K3;
+        const int kd = tp / (KS * KS), kh = (tp / KS) % KS, kw = tp % KS;
+        long long r = v;
+        const int ww = (int)(r % s.W); r /= s.W;
+        const int hh = (int)(r % s.H); r /= s.H;
+        const int dd = (int)(r % s.D); const int bb = (int)(r / s.D);
+        const int zd = dd + kd - R, zh = hh + kh - R, zw = ww + kw - R;
+        if (zd >= 0 && zd < s.D && zh >= 0 && zh < s.H && zw >= 0 && zw < s.W)
+          val = ld<TX>(x + ((size_t)bb * Cx + x_off + ci) * vol + (size_t)zd * plane + (size_t)zh * s.W + zw);
+      }
+      sb[kk][n] = val;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < WG_K; ++kk) {
+      const float a = sa[ty][kk];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[j] = fmaf(a, sb[kk][tx + 16 * j], acc[j]);
+    }
+  }
+  const int m = m0 + ty;
+  if (m >= Co) return;
+  for (int j = 0; j < 4; ++j) {
+    const int n = n0 + tx + 16 * j;
+    if (n < N) part[((size_t)blockIdx.z * Co + m) * N + n] = acc[j];
+  }
+}
+
+__global__ void k_wgrad_reduce(const float *__restrict__ part, int nchunk, long long n, float *__restrict__ g,
+                               int accumulate) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  float a = 0.f;
+  for (int c = 0; c < nchunk; ++c) a += part[(size_t)c * n + t];
+  g[t] = accumulate ? g[t] + a : a;
+}
+
+// db[co] (+)= sum over batch and voxels of dY (channel-offset view; one block per
+// channel, fixed summation order)
+__global__ void k_bias_grad(const float *__restrict__ dy, int Co, int Cdy, int dy_off, long long vol, int B,
+                            float *__restrict__ db, int accumulate) {
+  __shared__ float sh[256];
+  const int co = blockIdx.x;
+  float a = 0.f;
+  for (int b = 0; b < B; ++b)
+    for (long long v = threadIdx.x; v < vol; v += blockDim.x) a += dy[((size_t)b * Cdy + dy_off + co) * vol + v];
+  sh[threadIdx.x] = a;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) db[co] = accumulate ? db[co] + sh[0] : sh[0];
+}
+
+// dY *= (Y > 0) for a ReLU output Y; dY and Y are the same channel-offset view
+// (channels [co_off, co_off+C) of Cy-channel tensors)
+template <class TY>
+__global__ void k_relu_bwd(float *__restrict__ dy, const TY *__restrict__ y, int C, int Cy, int co_off, long long vol,
+                           int B) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)B * C * vol) return;
+  const long long v = t % vol, bc = t / vol;
+  const int c = (int)(bc % C), b = (int)(bc / C);
+  const size_t i = ((size_t)b * Cy + co_off + c) * vol + v;
+  if (!(ld<TY>(y + i) > 0.f)) dy[i] = 0.f;
+}
+
+// y[b][c] = x[b][c] * scale[b*C + c], optionally floored at zero
+template <class TI, class TO>
+__global__ void k_scale(const TI *__restrict__ x, TO *__restrict__ y, int C, long long vol, int B,
+                        const float *__restrict__ scale, int floor0) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)B * C * vol) return;
+  float r = ld<TI>(x + t) * scale[t / vol];
+  if (floor0) r = fmaxf(r, 0.f);
+  st<TO>(y + t, r);
+}
+
+// 2x2x2 average pooling of channels [src_off, src_off+C) of a Cs-channel tensor
+__global__ void k_pool2(const __nv_bfloat16 *__restrict__ x, int Cs, int src_off, __nv_bfloat16 *__restrict__ y, int C,
+                        Shape so) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)so.B * C * so.D * so.H * so.W;
+  if (t >= n) return;
+  long long r = t;
+  const int w = (int)(r % so.W); r /= so.W;
+  const int h = (int)(r % so.H); r /= so.H;
+  const int d = (int)(r % so.D); r /= so.D;
+  const int c = (int)(r % C), b = (int)(r / C);
+  const int W = so.W * 2, H = so.H * 2, D = so.D * 2;
+  const __nv_bfloat16 *xc = x + ((size_t)b * Cs + src_off + c) * D * H * W;
+  float a = 0.f;
+  for (int k = 0; k < 8; ++k)
+    a += __bfloat162float(xc[((size_t)(2 * d + (k >> 2)) * H + 2 * h + ((k >> 1) & 1)) * W + 2 * w + (k & 1)]);
+  y[t] = __float2bfloat16_rn(0.125f * a);
+}
+
+// gradient of k_pool2: dX (channels [dst_off, dst_off+C) of a Cd-channel tensor) += dY / 8
+__global__ void k_pool2_bwd(const float *__restrict__ dy, float *__restrict__ dx, int C, int Cd, int dst_off, Shape si) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)si.B * C * si.D * si.H * si.W;
+  if (t >= n) return;
+  long long r = t;
+  const int w = (int)(r % si.W); r /= si.W;
+  const int h = (int)(r % si.H); r /= si.H;
+  const int d = (int)(r % si.D); r /= si.D;
+  const int c = (int)(r % C), b = (int)(r / C);
+  const int Wo = si.W / 2, Ho = si.H / 2, Do = si.D / 2;
+  const float g = 0.125f * dy[((((size_t)b * C + c) * Do + d / 2) * Ho + h / 2) * Wo + w / 2];
+  dx[((((size_t)b * Cd + dst_off + c) * si.D + d) * si.H + h) * si.W + w] += g;
+}
+
+// nearest 2x upsampling into channels [dst_off, dst_off+C) of a Cd-channel tensor
+__global__ void k_up2(const __nv_bfloat16 *__restrict__ x, __nv_bfloat16 *__restrict__ y, int C, int Cd, int dst_off,
+                      Shape so) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)so.B * C * so.D * so.H * so.W;
+  if (t >= n) return;
+  long long r = t;
+  const int w = (int)(r % so.W); r /= so.W;
+  const int h = (int)(r % so.H); r /= so.H;
+  const int d = (int)(r % so.D); r /= so.D;
+  const int c = (int)(r % C), b = (int)(r / C);
+  const int Wi = so.W / 2, Hi = so.H / 2, Di = so.D / 2;
+  y[((((size_t)b * Cd + dst_off + c) * so.D + d) * so.H + h) * so.W + w] =
+      x[((((size_t)b * C + c) * Di + d / 2) * Hi + h / 2) * Wi + w / 2];
+}
+
+// gradient of k_up2: dX = sum of the 8 children of channels [src_off, src_off+C) of dY (Cs channels)
+__global__ void k_up2_bwd(const float *__restrict__ dy, int Cs, int src_off, float *__restrict__ dx, int C, Shape si) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)si.B * C * si.D * si.H * si.W;
+  if (t >= n) return;
+  long long r = t;
+  const int w = (int)(r % si.W); r /= si.W;
+  const int h = (int)(r % si.H); r /= si.H;
+  const int d = (int)(r % si.D); r /= si.D;
+  const int c = (int)(r % C), b = (int)(r / C);
+  const int W = si.W * 2, H = si.H * 2, D = si.D * 2;
+  const float *g = dy + ((size_t)b * Cs + src_off + c) * D * H * W;
+  float a = 0.f;
+  for (int k = 0; k < 8; ++k) a += g[((size_t)(2 * d + (k >> 2)) * H + 2 * h + ((k >> 1) & 1)) * W + 2 * w + (k & 1)];
+  dx[t] = a;
+}
+
+// mean squared error: per-block partial sums of (p - q)^2 and dP = 2 (p - q) / n
+__global__ void k_mse(const float *__restrict__ p, const float *__restrict__ q, long long n, float *__restrict__ dp,
+                      float *__restrict__ part) {
+  __shared__ float sh[256];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  float e = 0.f;
+  if (t < n) {
+    const float r = p[t] - q[t];
+    e = r * r;
+    dp[t] = 2.f * r / (float)n;
+  }
+  sh[threadIdx.x] = e;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// Adam on FP32 master weights; the BF16 working copy is refreshed
+__global__ void k_adam(float *__restrict__ wm, __nv_bfloat16 *__restrict__ wb, const float *__restrict__ g,
+                       float *__restrict__ m, float *__restrict__ v, long long n, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const float gt = g[t];
+  const float mt = b1 * m[t] + (1.f - b1) * gt;
+  const float vt = b2 * v[t] + (1.f - b2) * gt * gt;
+  m[t] = mt;
+  v[t] = vt;
+  const float w = wm[t] - lr * (mt / c1) / (sqrtf(vt / c2) + eps);
+  wm[t] = w;
+  if (wb) wb[t] = __float2bfloat16_rn(w);
+}
+
+__global__ void k_cast_f2b(const float *__restrict__ a, __nv_bfloat16 *__restrict__ b, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) b[t] = __float2bfloat16_rn(a[t]);
+}
+
+__global__ void k_cast_b2f(const __nv_bfloat16 *__restrict__ a, float *__restrict__ b, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) b[t] = __bfloat162float(a[t]);
+}
+
+inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+template <class TI, class TO, int KS, int CO_T>
+cudaError_t conv_t(const void *x, int Ci, int Cx, int x_off, const void *w, const float *bias, void *y, int Co, int Cy,
+                   int co_off, Shape s, int relu, int accumulate, cudaStream_t st) {
+  constexpr int VX = 4;
+  if (s.W % VX != 0) return cudaErrorInvalidValue;
+  dim3 g(nblk((long long)s.B * s.D * s.H * (s.W / VX), 128), (Co + CO_T - 1) / CO_T);
+  k_conv3d<TI, TO, KS, CO_T, VX><<<g, 128, 0, st>>>((const TI *)x, Ci, Cx, x_off, (const __nv_bfloat16 *)w, bias,
+                                                     (TO *)y, Co, Cy, co_off, s, relu, accumulate);
+  return cudaGetLastError();
+}
+
+template <class TI, class TO>
+cudaError_t conv_k(int ks, const void *x, int Ci, int Cx, int x_off, const void *w, const float *bias, void *y, int Co,
+                   int Cy, int co_off, Shape s, int relu, int accumulate, cudaStream_t st) {
+  if (ks == 3) return conv_t<TI, TO, 3, 8>(x, Ci, Cx, x_off, w, bias, y, Co, Cy, co_off, s, relu, accumulate, st);
+  if (ks == 1) return conv_t<TI, TO, 1, 8>(x, Ci, Cx, x_off, w, bias, y, Co, Cy, co_off, s, relu, accumulate, st);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+namespace gt {
+int set_error(int code, const char *msg);
+int cuda_error(cudaError_t e, const char *what, int line);
+}  // namespace gt
+
+#define NN_CK(expr, what)                                              \
+  do {                                                                 \
+    cudaError_t e_ = (expr);                                           \
+    if (e_ != cudaSuccess) return gt::cuda_error(e_, what, __LINE__);   \
+  } while (0)
+
+extern "C" {
+
+// dtype codes: 0 = float32, 1 = bfloat16
+int gt_nn_conv3d(const void *x, int x_dtype, int Ci, int Cx, int x_off, const void *w_bf16, const float *bias, void *y,
+                 int y_dtype, int Co, int Cy, int co_off, int B, int D, int H, int W, int ksize, int relu,
+                 int accumulate, void *stream) {
+  if (!x || !w_bf16 || !y || Ci < 1 || Co < 1 || co_off < 0 || co_off + Co > Cy || x_off < 0 || x_off + Ci > Cx)
+    return gt::set_error(GT_ERR_ARG, "gt_nn_conv3d: bad argument");
+  if (B < 1 || D < 1 || H < 1 || W < 4 || W % 4 != 0 || (ksize != 1 && ksize != 3))
+    return gt::set_error(GT_ERR_ARG, "gt_nn_conv3d: shape must be positive with W % 4 == 0, ksize 1 or 3");
+  const Shape s{B, D, H, W};
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  if (x_dtype == 1 && y_dtype == 1)
+    e = conv_k<__nv_bfloat16, __nv_bfloat16>(ksize, x, Ci, Cx, x_off, w_bf16, bias, y, Co, Cy, co_off, s, relu, accumulate, st);
+  else if (x_dtype == 1 && y_dtype == 0)
+    e = conv_k<__nv_bfloat16, float>(ksize, x, Ci, Cx, x_off, w_bf16, bias, y, Co, Cy, co_off, s, relu, accumulate, st);
+  else if (x_dtype == 0 && y_dtype == 0)
+    e = conv_k<float, float>(ksize, x, Ci, Cx, x_off, w_bf16, bias, y, Co, Cy, co_off, s, relu, accumulate, st);
+  else if (x_dtype == 0 && y_dtype == 1)
+    e = conv_k<float, __nv_bfloat16>(ksize, x, Ci, Cx, x_off, w_bf16, bias, y, Co, Cy, co_off, s, relu, accumulate, st);
+  else
+    return gt::set_error(GT_ERR_ARG, "gt_nn_conv3d: dtype must be 0 (f32) or 1 (bf16)");
+  NN_CK(e, "gt_nn_conv3d");
+  return GT_OK;
+}
+
+int gt_nn_flip_weights(const void *w_bf16, void *wf_bf16, int Co, int Ci, int ksize, void *stream) {
+  const int K3 = ksize * ksize * ksize;
+  k_flip<<<nblk((long long)Co * Ci * K3, 256), 256, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16 *)w_bf16, (__nv_bfloat16 *)wf_bf16, Co, Ci, K3);
+  NN_CK(cudaGetLastError(), "gt_nn_flip_weights");
+  return GT_OK;
+}
+
+// part must hold nchunk * Co * Ci * K3 floats; nchunk = ceil(voxels / kchunk)
+int gt_nn_conv3d_wgrad(const float *dy, int Co, int Cdy, int dy_off, const void *x, int x_dtype, int Ci, int Cx,
+                       int x_off, int B, int D, int H, int W, int ksize, long long kchunk, float *part, float *g,
+                       int accumulate, void *stream) {
+  if (!dy || !x || !part || !g || kchunk < 1 || dy_off < 0 || dy_off + Co > Cdy || x_off < 0 || x_off + Ci > Cx)
+    return gt::set_error(GT_ERR_ARG, "gt_nn_conv3d_wgrad: bad argument");
+  const int K3 = ksize * ksize * ksize, N = Ci * K3;
+  const long long nvox = (long long)B * D * H * W;
+  const long long nchunk = (nvox + kchunk - 1) / kchunk;
+  if (nchunk > 65535) return gt::set_error(GT_ERR_ARG, "gt_nn_conv3d_wgrad: kchunk too small (more than 65535 chunks)");
+  const Shape s{B, D, H, W};
+  cudaStream_t st = (cudaStream_t)stream;
+  dim3 grid(nblk(N, WG_N), nblk(Co, WG_M), (unsigned)nchunk);
+  if (ksize == 3 && x_dtype == 1)
+    k_wgrad<__nv_bfloat16, 3><<<grid, 256, 0, st>>>(dy, Co, Cdy, dy_off, (const __nv_bfloat16 *)x, Ci, Cx, x_off, s, kchunk, part);
+  else if (ksize == 1 && x_dtype == 1)
+    k_wgrad<__nv_bfloat16, 1><<<grid, 256, 0, st>>>(dy, Co, Cdy, dy_off, (const __nv_bfloat16 *)x, Ci, Cx, x_off, s, kchunk, part);
+  else if (ksize == 3 && x_dtype == 0)
+    k_wgrad<float, 3><<<grid, 256, 0, st>>>(dy, Co, Cdy, dy_off, (const float *)x, Ci, Cx, x_off, s, kchunk, part);
+  else if (ksize == 1 && x_dtype == 0)
+    k_wgrad<float, 1><<<grid, 256, 0, st>>>(dy, Co, Cdy, dy_off, (const float *)x, Ci, Cx, x_off, s, kchunk, part);
+  else
+    return gt::set_error(GT_ERR_ARG, "gt_nn_conv3d_wgrad: ksize 1 or 3, dtype 0 or 1");
+  const long long n = (long long)Co * N;
+  k_wgrad_reduce<<<nblk(n, 256), 256, 0, st>>>(part, (int)nchunk, n, g, accumulate);
+  NN_CK(cudaGetLastError(), "gt_nn_conv3d_wgrad");
+  return GT_OK;
+}
+
+int gt_nn_bias_grad(const float *dy, int Co, int Cdy, int dy_off, int B, long long vol, float *db, int accumulate,
+                    void *stream) {
+  if (!dy || !db || Co < 1 || dy_off < 0 || dy_off + Co > Cdy) return gt::set_error(GT_ERR_ARG, "gt_nn_bias_grad: bad argument");
+  k_bias_grad<<<Co, 256, 0, (cudaStream_t)stream>>>(dy, Co, Cdy, dy_off, vol, B, db, accumulate);
+  NN_CK(cudaGetLastError(), "gt_nn_bias_grad");
+  return GT_OK;
+}
+
+int gt_nn_scale(const void *x, int x_dtype, void *y, int y_dtype, int C, int B, long long vol, const float *scale,
+                int floor0, void *stream) {
+  if (!x || !y || !scale || C < 1 || B < 1 || vol < 1) return gt::set_error(GT_ERR_ARG, "gt_nn_scale: bad argument");
+  const long long n = (long long)B * C * vol;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (x_dtype == 0 && y_dtype == 0) k_scale<float, float><<<nblk(n, 256), 256, 0, st>>>((const float *)x, (float *)y, C, vol, B, scale, floor0);
+  else if (x_dtype == 0 && y_dtype == 1) k_scale<float, __nv_bfloat16><<<nblk(n, 256), 256, 0, st>>>((const float *)x, (__nv_bfloat16 *)y, C, vol, B, scale, floor0);
+  else if (x_dtype == 1 && y_dtype == 0) k_scale<__nv_bfloat16, float><<<nblk(n, 256), 256, 0, st>>>((const __nv_bfloat16 *)x, (float *)y, C, vol, B, scale, floor0);
+  else if (x_dtype == 1 && y_dtype == 1) k_scale<__nv_bfloat16, __nv_bfloat16><<<nblk(n, 256), 256, 0, st>>>((const __nv_bfloat16 *)x, (__nv_bfloat16 *)y, C, vol, B, scale, floor0);
+  else return gt::set_error(GT_ERR_ARG, "gt_nn_scale: dtype must be 0 (f32) or 1 (bf16)");
+  NN_CK(cudaGetLastError(), "gt_nn_scale");
+  return GT_OK;
+}
+
+int gt_nn_relu_bwd(float *dy, const void *y, int y_dtype, int C, int Cy, int co_off, int B, long long vol,
+                   void *stream) {
+  const long long n = (long long)B * C * vol;
+  if (y_dtype == 1) k_relu_bwd<__nv_bfloat16><<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>(dy, (const __nv_bfloat16 *)y, C, Cy, co_off, vol, B);
+  else k_relu_bwd<float><<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>(dy, (const float *)y, C, Cy, co_off, vol, B);
+  NN_CK(cudaGetLastError(), "gt_nn_relu_bwd");
+  return GT_OK;
+}
+
+int gt_nn_pool2(const void *x_bf16, int Cs, int src_off, void *y_bf16, int C, int B, int Do, int Ho, int Wo,
+                void *stream) {
+  const Shape so{B, Do, Ho, Wo};
+  k_pool2<<<nblk((long long)B * C * Do * Ho * Wo, 256), 256, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16 *)x_bf16, Cs, src_off, (__nv_bfloat16 *)y_bf16, C, so);
+  NN_CK(cudaGetLastError(), "gt_nn_pool2");
+  return GT_OK;
+}
+
+int gt_nn_pool2_bwd(const float *dy, float *dx, int C, int Cd, int dst_off, int B, int D, int H, int W, void *stream) {
+  const Shape si{B, D, H, W};
+  k_pool2_bwd<<<nblk((long long)B * C * D * H * W, 256), 256, 0, (cudaStream_t)stream>>>(dy, dx, C, Cd, dst_off, si);
+  NN_CK(cudaGetLastError(), "gt_nn_pool2_bwd");
+  return GT_OK;
+}
+
+int gt_nn_up2(const void *x_bf16, void *y_bf16, int C, int Cd, int dst_off, int B, int D, int H, int W, void *stream) {
+  const Shape so{B, D, H, W};
+  k_up2<<<nblk((long long)B * C * D * H * W, 256), 256, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16 *)x_bf16, (__nv_bfloat16 *)y_bf16, C, Cd, dst_off, so);
+  NN_CK(cudaGetLastError(), "gt_nn_up2");
+  return GT_OK;
+}
+
+int gt_nn_up2_bwd(const float *dy, int Cs, int src_off, float *dx, int C, int B, int Di, int Hi, int Wi,
+                  void *stream) {
+  const Shape si{B, Di, Hi, Wi};
+  k_up2_bwd<<<nblk((long long)B * C * Di * Hi * Wi, 256), 256, 0, (cudaStream_t)stream>>>(dy, Cs, src_off, dx, C, si);
+  NN_CK(cudaGetLastError(), "gt_nn_up2_bwd");
+  return GT_OK;
+}
+
+// part must hold ceil(n/256) floats
+int gt_nn_mse(const float *p, const float *q, long long n, float *dp, float *part, void *stream) {
+  k_mse<<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>(p, q, n, dp, part);
+  NN_CK(cudaGetLastError(), "gt_nn_mse");
+  return GT_OK;
+}
+
+int gt_nn_adam(float *w_master, void *w_bf16, const float *g, float *m, float *v, long long n, float lr, float b1,
+               float b2, float eps, int step, void *stream) {
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  k_adam<<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>(w_master, (__nv_bfloat16 *)w_bf16, g, m, v, n, lr, b1, b2,
+                                                         eps, c1, c2);
+  NN_CK(cudaGetLastError(), "gt_nn_adam");
+  return GT_OK;
+}
+
+int gt_nn_cast(const void *src, int src_dtype, void *dst, long long n, void *stream) {
+  if (src_dtype == 0) k_cast_f2b<<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>((const float *)src, (__nv_bfloat16 *)dst, n);
+  else k_cast_b2f<<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)src, (float *)dst, n);
+  NN_CK(cudaGetLastError(), "gt_nn_cast");
+  return GT_OK;
+}
+
+}  // extern "C"

@@ -131,6 +131,16 @@ class Problem:
         a = np.ascontiguousarray(value, dtype=np.float32).reshape(self._shape(field))
         L.check(L.lib().gt_set_state(self._h, L.FIELDS[field], _ptr(a)))
 
+    def set_tuning(self, fwd: int, bp: int):
+        """Force the projector launch configurations (see gt_set_tuning)."""
+        L.check(L.lib().gt_set_tuning(self._h, int(fwd), int(bp)))
+        return self
+
+    def dual_from_primal(self):
+        """Set lambda consistent with the current u (for warm starts)."""
+        L.check(L.lib().gt_dual_from_primal(self._h))
+        return self
+
     @property
     def scalars(self) -> dict:
         out = (ctypes.c_double * 4)()

@@ -101,6 +101,9 @@ GT_API int gt_set_state(gt_problem *p, int field, const float *host);
 /* Launch shapes the autotuner chose: [0] forward projector, [1] back projector
  * (indices into the configurations listed at launch_fwd / launch_bp). */
 GT_API int gt_get_tuning(gt_problem *p, int out[2]);
+/* Force the projector launch shapes (for tests and measurements); the values
+ * range over the configurations listed at launch_fwd / launch_bp. */
+GT_API int gt_set_tuning(gt_problem *p, int fwd_cfg, int bp_cfg);
 
 /* Scalars the run uses: [0] normest, [1] sigma, [2] tau, [3] iterations run. */
 GT_API int gt_get_scalars(gt_problem *p, double out[4]);
@@ -170,6 +173,77 @@ GT_API int gt_batch_invalidate(gt_batch *b);
 /* Run the batch's problems on `chains` concurrent chains (problem k on chain
  * k mod chains, one after another within a chain); default 8. */
 GT_API int gt_batch_set_concurrency(gt_batch *b, int chains);
+
+/* Kernels of the learned warm start (a small 3-D U-Net whose output initialises
+ * the solver's image).  No counterpart in the reference, which always starts
+ * from zero (radon_tgv_primal_dual_3d.py:1147-1176).  All pointers are device
+ * pointers; tensors are [B][C][D][H][W] with W fastest; dtype codes are
+ * 0 = float32, 1 = bfloat16.  Weights are bfloat16 [Co][Ci][k][k][k] (k = 1 or 3),
+ * biases float32; every sum accumulates in float32.  Calls are asynchronous on
+ * `stream`.
+ *
+ * A tensor argument is a channel-offset view: channels [off, off+C) of a tensor
+ * with Ctot channels (x: Cx / x_off, y: Cy / co_off, dy: Cdy / dy_off), so the
+ * U-Net's skip concatenations need no copies.
+ *
+ * gt_nn_conv3d: y view = conv(x view, w) + bias, optionally ReLU'd (relu = 1)
+ *   and added to y first (accumulate = 1); W % 4 == 0.  With the weights of
+ *   gt_nn_flip_weights, no bias and dy as x, it gives the data gradient.
+ * gt_nn_flip_weights: wf[ci][co][t] = w[co][ci][k^3-1-t].
+ * gt_nn_conv3d_wgrad: g[co][ci][t] (+)= sum over batch and voxels of
+ *   dy[co] * x[ci] shifted by tap t; `part` holds ceil(B*D*H*W / kchunk)*Co*Ci*k^3
+ *   floats of partial sums, reduced in a fixed order (deterministic).
+ * gt_nn_bias_grad: db[co] (+)= sum of dy[:, co].
+ * gt_nn_scale: y[b][c] = x[b][c] * scale[b*C + c] (scale on the device),
+ *   floored at zero when floor0 = 1; also converts between dtypes.
+ * gt_nn_relu_bwd: dy = 0 where y is not > 0 (dy and y: the same view).
+ * gt_nn_pool2 / gt_nn_pool2_bwd: 2x2x2 average pooling of channels
+ *   [off, off+C) of a wider tensor, and its gradient (added into dx).
+ * gt_nn_up2 / gt_nn_up2_bwd: nearest 2x upsampling into channels [off, off+C)
+ *   of a wider tensor, and its gradient.
+ * gt_nn_mse: dp = 2 (p - q) / n and per-256-block partial sums of (p - q)^2
+ *   (ceil(n/256) floats in part).
+ * gt_nn_adam: Adam step (bias-corrected, step >= 1) on float32 master weights,
+ *   refreshing the bfloat16 copy when w_bf16 is not NULL.
+ * gt_nn_cast: float32 <-> bfloat16 (src_dtype 0: f32 -> bf16, 1: bf16 -> f32). */
+GT_API int gt_nn_conv3d(const void *x, int x_dtype, int Ci, int Cx, int x_off, const void *w_bf16, const float *bias,
+                        void *y, int y_dtype, int Co, int Cy, int co_off, int B, int D, int H, int W, int ksize,
+                        int relu, int accumulate, void *stream);
+GT_API int gt_nn_flip_weights(const void *w_bf16, void *wf_bf16, int Co, int Ci, int ksize, void *stream);
+GT_API int gt_nn_conv3d_wgrad(const float *dy, int Co, int Cdy, int dy_off, const void *x, int x_dtype, int Ci, int Cx,
+                              int x_off, int B, int D, int H, int W, int ksize, long long kchunk, float *part,
+                              float *g, int accumulate, void *stream);
+GT_API int gt_nn_bias_grad(const float *dy, int Co, int Cdy, int dy_off, int B, long long vol, float *db,
+                           int accumulate, void *stream);
+GT_API int gt_nn_scale(const void *x, int x_dtype, void *y, int y_dtype, int C, int B, long long vol,
+                       const float *scale, int floor0, void *stream);
+GT_API int gt_nn_relu_bwd(float *dy, const void *y, int y_dtype, int C, int Cy, int co_off, int B, long long vol,
+                          void *stream);
+GT_API int gt_nn_pool2(const void *x_bf16, int Cs, int src_off, void *y_bf16, int C, int B, int Do, int Ho, int Wo,
+                       void *stream);
+GT_API int gt_nn_pool2_bwd(const float *dy, float *dx, int C, int Cd, int dst_off, int B, int D, int H, int W,
+                           void *stream);
+GT_API int gt_nn_up2(const void *x_bf16, void *y_bf16, int C, int Cd, int dst_off, int B, int D, int H, int W,
+                     void *stream);
+GT_API int gt_nn_up2_bwd(const float *dy, int Cs, int src_off, float *dx, int C, int B, int Di, int Hi, int Wi,
+                         void *stream);
+GT_API int gt_nn_mse(const float *p, const float *q, long long n, float *dp, float *part, void *stream);
+GT_API int gt_nn_adam(float *w_master, void *w_bf16, const float *g, float *m, float *v, long long n, float lr,
+                      float b1, float b2, float eps, int step, void *stream);
+GT_API int gt_nn_cast(const void *src, int src_dtype, void *dst, long long n, void *stream);
+
+/* Device-side state access (for the warm start): like gt_get_state /
+ * gt_set_state, in the same [comps][S][X] order, but to / from a device buffer,
+ * asynchronous on the problem's stream (no host synchronisation). */
+GT_API int gt_get_state_device(gt_problem *p, int field, float *dev);
+GT_API int gt_set_state_device(gt_problem *p, int field, const float *dev);
+/* Set the data dual lambda to the value consistent with the current u: the fixed
+ * point of the reference's lambda update for K u (KL: mu (1 - f / K u), kept
+ * where K u <= 0; L2: mu (K u - f)).  For warm starts (set u, then this).  No
+ * counterpart in the reference, which starts lambda at zero. */
+GT_API int gt_dual_from_primal(gt_problem *p);
+/* The problem's CUDA stream (the one gt_desc.stream named, or its own). */
+GT_API void *gt_problem_stream(gt_problem *p);
 
 /* Number of kernel launches one iteration issues (for launch accounting). */
 GT_API int gt_launches_per_iteration(const gt_problem *p);
