@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 W = dict(N=256, Nz=60, C=4, nang=71, alpha=(4.0, 1.0), mu=[0.2, 5e-4, 4e-3, 5e-4], peaks=[1e4, 20.0, 20.0, 20.0],
          stated_iterations=2500)
 METRIC = "voxel-iter/s"
-WORKLOAD_NAME = "3D FROB3D TGV-KL {N}x{N}x{Nz}, 4 channels, {N} bins x 71 angles"
+WORKLOAD_NAME = "3D FROB3D TGV-KL {N}x{N}x{Nz}, 4 channels, {N} bins x {nang} angles"
 
 
 def peaks():
@@ -223,7 +223,7 @@ def run_reference(args, rank, world):
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"]), "sample_slices": Nz},
+            "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"], nang=W["nang"]), "sample_slices": Nz},
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": os.cpu_count(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -265,7 +265,7 @@ def run_ours(args, rank, world, local):
         prob.close()
         return {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-                "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"]), "Nz": Nz, "quick": True}, "clocks": clocks}
+                "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"], nang=W["nang"]), "Nz": Nz, "quick": True}, "clocks": clocks}
 
     # ---- per-kernel durations (CUDA events on the launching stream) for the roofline
     kms = prob.time_kernels(reps=5)
@@ -300,11 +300,11 @@ def run_ours(args, rank, world, local):
     out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": it_ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantoms, Poisson noise)",
-           "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"]), "voxel_channels": V, "sinogram_bins": Sb, "dim": 3, "N": N,
+           "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"], nang=W["nang"]), "voxel_channels": V, "sinogram_bins": Sb, "dim": 3, "N": N,
                       "Nz": Nz, "C": C, "nang": nang, "coupling": "FROB", "discrepancy": "KL",
                       "regularisation": "TGV", "stated_iterations": W["stated_iterations"],
                       "time_for_stated_iterations_s": it_ms * W["stated_iterations"] / 1e3,
-                      "l2": "inputs larger than L2 (solver state 1.1 GB per replica)",
+                      "l2": f"inputs larger than L2 (solver state {V * 76 / 1e9:.1f} GB per replica)",
                       "parallelism": f"replicas x{world}", "normest": ne, "autotuned": tuning},
            "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                         "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
@@ -429,6 +429,8 @@ def main():
     ap.add_argument("--nz", type=int, default=None,
                     help="slices per channel (default 60); smaller cases for profiler captures")
     ap.add_argument("--n", type=int, default=None, help="image side (default 256); profiler captures")
+    ap.add_argument("--nang", type=int, default=None,
+                    help="projection angles (default 71; the 768^2 x 384 large run uses 141)")
     ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched"],
                     help="coupled3d: the 3-D 4-channel workload (default); batched: 64 uneven problems")
     ap.add_argument("--batch", type=int, default=64, help="problems per rank for --workload batched")
@@ -439,6 +441,8 @@ def main():
         W["Nz"] = int(args.nz)
     if args.n:
         W["N"] = int(args.n)
+    if args.nang:
+        W["nang"] = int(args.nang)
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         out = run_reference(args, rank, world)

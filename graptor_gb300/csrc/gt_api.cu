@@ -235,7 +235,11 @@ int autotune(gt_problem *p) {
   for (int round = 0; round < 4 && rc == GT_OK; ++round) {
     for (int which = 0; which < 2 && rc == GT_OK; ++which) {
       const int nc = which == 0 ? ncf : ncb;
+      float best_ms = 1e30f;
+      for (int c = 0; c < nc; ++c) best_ms = std::min(best_ms, ms_cfg[which][c]);
       for (int c = 0; c < nc && rc == GT_OK; ++c) {
+        // after the first round only configurations within 30 % of the best are timed again
+        if (round > 0 && ms_cfg[which][c] > 1.3f * best_ms) continue;
         gt::IterParams Q = p->P;
         if (which == 0) Q.fwd_cfg = c; else Q.bp_cfg = c;
         auto launch = [&]() { return which == 0 ? gt::launch_fwd(Q, p->disc, p->stream) : gt::launch_bp(Q, p->stream); };

@@ -975,6 +975,76 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
   }
 }
 
+// Back projection of R consecutive pixels of one row at once.  Along a row the
+// detector coordinate moves by X = cos(angle) per pixel (|X| <= 1), so the R
+// pixels' taps span about R|X| + 2 bins: the pixels are visited in the order in
+// which their bins increase and the two current taps slide along, each bin loaded
+// once per angle.  Every pixel adds its taps in the reference's order (angles
+// ascending, lower tap then upper tap) with the reference's interpolation weights.
+template <int VW, int R, bool REV>
+__device__ __forceinline__ void bp_run_angle(const float *__restrict__ lj, size_t S, int nd, float fnd, const float4 o,
+                                             int x0, float yf, int N, const Slices<VW> &sl, float (&acc)[R][VW]) {
+  int cur = -3;  // bins held: A = cur, B = cur + 1
+  float A[VW], Bv[VW];
+#pragma unroll
+  for (int k = 0; k < VW; ++k) { A[k] = 0.f; Bv[k] = 0.f; }
+#pragma unroll
+  for (int rr = 0; rr < R; ++rr) {
+    const int r = REV ? R - 1 - rr : rr;
+    if (x0 + r >= N) continue;
+    const float xf = (float)(x0 + r);
+    const float tt = __fadd_rn(__fadd_rn(__fmul_rn(xf, o.x), __fmul_rn(yf, o.y)), o.z);
+    if (!(tt > -1.f && tt < fnd)) continue;
+    const float fl = floorf(tt);
+    const float p = fminf(__fsub_rn(tt, fl), 0x1.fffffep-1f);
+    const float q = __fsub_rn(1.0f, p);
+    const int il = (int)fl;
+    if (il != cur) {
+      if (il == cur + 1) {
+#pragma unroll
+        for (int k = 0; k < VW; ++k) A[k] = Bv[k];
+      } else if (il >= 0) {
+        sl.load(lj + (size_t)il * S, A);
+      }
+      if (il <= nd - 2) sl.load(lj + (size_t)(il + 1) * S, Bv);
+      cur = il;
+    }
+    if (il >= 0) {
+#pragma unroll
+      for (int k = 0; k < VW; ++k) acc[r][k] = __fmaf_rn(q, A[k], acc[r][k]);
+    }
+    if (il <= nd - 2) {
+#pragma unroll
+      for (int k = 0; k < VW; ++k) acc[r][k] = __fmaf_rn(p, Bv[k], acc[r][k]);
+    }
+  }
+}
+
+template <int VW, int R>
+__global__ void __launch_bounds__(256) k_bp_run(const IterParams P) {
+  const Dims d = P.d;
+  const int nrun = (d.N + R - 1) / R;
+  long long unit;
+  Slices<VW> sl;
+  if (!map_thread<VW>((long long)d.N * nrun, d.S, unit, sl)) return;
+  const int y = (int)(unit / nrun), x0 = (int)(unit - (long long)y * nrun) * R;
+  float acc[R][VW];
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int k = 0; k < VW; ++k) acc[r][k] = 0.f;
+  const float fnd = (float)d.nd, yf = (float)y;
+  for (int j = 0; j < d.nang; ++j) {
+    const float4 o = __ldg(P.ofs + j);
+    const float *lj = P.lam + (size_t)j * d.nd * d.S;
+    if (o.x < 0.f) bp_run_angle<VW, R, true>(lj, d.S, d.nd, fnd, o, x0, yf, d.N, sl, acc);
+    else bp_run_angle<VW, R, false>(lj, d.S, d.nd, fnd, o, x0, yf, d.N, sl, acc);
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (x0 + r < d.N) sl.store(P.kstar + ((size_t)y * d.N + x0 + r) * d.S, acc[r]);
+}
+
 // k_bp: back projection K* lambda of every (pixel, slice) into P.kstar; it only
 // needs lambda, so it runs beside k_dual.
 template <int VW, int AU, bool TAB>
@@ -1473,17 +1543,25 @@ __device__ __forceinline__ void radon_run(const float *__restrict__ img, size_t 
       if (a <= b) { xmin = min(xmin, a); xmax = max(xmax, b); }
     }
     const float *row = img + (size_t)y * N * S;
-#pragma unroll 2
-    for (int x = xmin; x <= xmax; ++x) {
-      float val[VW];
-      sl.load(row + (size_t)x * S, val);
-      const float tx = __fadd_rn(__fmul_rn((float)x, o.x), d);
+    // groups of G pixels: their loads are issued together, then consumed in x order
+    constexpr int G = 4;
+    for (int xg = xmin; xg <= xmax; xg += G) {
+      float val[G][VW];
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const float wgt = 1.0f - fabsf(__fsub_rn(tx, (float)(i0 + r)));
-        if (x >= xl[r] && x <= xh[r] && wgt > 0.f) {
+      for (int g = 0; g < G; ++g)
+        if (xg + g <= xmax) sl.load(row + (size_t)(xg + g) * S, val[g]);
 #pragma unroll
-          for (int k = 0; k < VW; ++k) acc[r][k] = mac<EXACT>(acc[r][k], wgt, val[k]);
+      for (int g = 0; g < G; ++g) {
+        const int x = xg + g;
+        if (x > xmax) break;
+        const float tx = __fadd_rn(__fmul_rn((float)x, o.x), d);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const float wgt = 1.0f - fabsf(__fsub_rn(tx, (float)(i0 + r)));
+          if (x >= xl[r] && x <= xh[r] && wgt > 0.f) {
+#pragma unroll
+            for (int k = 0; k < VW; ++k) acc[r][k] = mac<EXACT>(acc[r][k], wgt, val[g][k]);
+          }
         }
       }
     }
@@ -1538,14 +1616,14 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // (4, 4), (4, 8);
 // k_bp configs 0..7 = (slices per lane, angles per step, geometry) = (8, 2, table),
 // (8, 4, table), (4, 2, table), (4, 4, table), (8, 1, on the fly), (4, 1, on the fly),
-// (8, 2, on the fly), (4, 2, on the fly).
+// (8, 2, on the fly), (4, 2, on the fly); configs 9..12 = (slices per lane,
+// pixels per run) of k_bp_run = (8, 4), (4, 8), (8, 8), (4, 4).
 // Otherwise one fixed shape with 2 or 1 slices per thread.
-// For S a multiple of 4 up to 64, one more candidate each: one slice per thread
-// (k_fwd config 4, k_bp config 8), which keeps all lanes busy when S is small.
+// One more candidate each: one slice per thread (k_fwd config 4, k_bp config 8),
+// which keeps all lanes busy when S is small.
 int num_proj_configs(int S, int which) {
   if (S % 4 != 0) return 1;
-  if (which == 0) return 9;  // config 4 (one slice per thread) is kept as a candidate for every S
-  return S <= 64 ? 9 : 8;
+  return which == 0 ? 9 : 13;  // configs 4 / 8 (one slice per thread) stay candidates for every S
 }
 
 template <int VW, int UNR>
@@ -1590,6 +1668,12 @@ static void bp_vw(const IterParams &P, cudaStream_t st) {
   k_bp<VW, AU, TAB><<<blocks_for(threads_for<VW>((long long)P.d.N * P.d.N, P.d.S), 256), 256, 0, st>>>(P);
 }
 
+template <int VW, int R>
+static void bp_run(const IterParams &P, cudaStream_t st) {
+  const long long units = (long long)P.d.N * ((P.d.N + R - 1) / R);
+  k_bp_run<VW, R><<<blocks_for(threads_for<VW>(units, P.d.S), 256), 256, 0, st>>>(P);
+}
+
 cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
   const int S = P.d.S;
   if (S % 4 == 0) {
@@ -1602,6 +1686,10 @@ cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
       case 6: bp_vw<8, 2, false>(P, st); break;
       case 7: bp_vw<4, 2, false>(P, st); break;
       case 8: bp_vw<1, 1, false>(P, st); break;
+      case 9: bp_run<8, 4>(P, st); break;
+      case 10: bp_run<4, 8>(P, st); break;
+      case 11: bp_run<8, 8>(P, st); break;
+      case 12: bp_run<4, 4>(P, st); break;
       default: bp_vw<8, 2>(P, st); break;
     }
   } else if (S % 2 == 0) {

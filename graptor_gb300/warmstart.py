@@ -335,10 +335,24 @@ class WarmStarter:
     fixed point of its update for the predicted u (gt_dual_from_primal): without
     that the first iterations pull u back towards the cold-start state."""
 
-    def __init__(self, net: UNet3D, fields=("u", "v"), pre_iters: int = 20):
+    def __init__(self, net: UNet3D, fields=("u", "v"), pre_iters: int = 20, use=None, reset_dual: bool = True):
         self.net, self.fields, self.pre_iters = net, tuple(fields), int(pre_iters)
+        self.use = tuple(use) if use is not None else self.fields  # predicted fields written to the solver
+        self.reset_dual = bool(reset_dual)
         if self.fields[0] != "u":
             raise ValueError("the first predicted field must be u (the residual channels)")
+
+    def predict(self, x_norm: np.ndarray) -> np.ndarray:
+        """Network output (normalised fields) for a normalised input u [C][Nz][N][N]."""
+        import torch
+        net = self.net
+        C, Nz, N = x_norm.shape[0], x_norm.shape[1], x_norm.shape[2]
+        x = torch.from_numpy(np.ascontiguousarray(x_norm, np.float32)).to(net.dev).to(torch.bfloat16)[None]
+        out = torch.empty((1, net.cout, Nz, N, N), dtype=torch.float32, device=net.dev)
+        net.residual_base(x, out)
+        net.forward(x, out)
+        torch.cuda.synchronize(net.dev)
+        return out[0].cpu().numpy()
 
     def apply(self, prob, f: np.ndarray):
         import torch
@@ -375,12 +389,14 @@ class WarmStarter:
             dst = ctypes.c_void_p(res.data_ptr() + 4 * ch * vol)
             _ck(lib.gt_nn_scale(src, F32, dst, F32, n, 1, vol, ctypes.c_void_p(back.data_ptr() + 4 * ch),
                                 int(fl == "u"), st))
-            _ck(lib.gt_set_state_device(prob._h, L.FIELDS[fl], dst))
-            if fl in PAIRED:
-                _ck(lib.gt_set_state_device(prob._h, L.FIELDS[PAIRED[fl]], dst))
+            if fl in self.use:
+                _ck(lib.gt_set_state_device(prob._h, L.FIELDS[fl], dst))
+                if fl in PAIRED:
+                    _ck(lib.gt_set_state_device(prob._h, L.FIELDS[PAIRED[fl]], dst))
             ch += n
         # the data dual consistent with the predicted image (fixed point of its update)
-        _ck(lib.gt_dual_from_primal(prob._h))
+        if self.reset_dual:
+            _ck(lib.gt_dual_from_primal(prob._h))
         prob.synchronize()
         return prob
 

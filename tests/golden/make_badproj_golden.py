@@ -1,0 +1,78 @@
+"""Golden vectors for the bad-projection detector, from the REFERENCE's own code.
+
+    python tests/golden/make_badproj_golden.py
+
+Imports the reference's ``find_bad_ele.py`` (``GRAPTOR_REFERENCE``, default the
+reference checkout) with stand-ins for the modules it imports but does not use on
+this path (``h5utilities`` -- only its ``Brightness_correction`` is called, and it
+is replaced by a function returning the seeded input stack -- ``mrcfile``,
+``scipy.misc`` and ``matplotlib``), then records its helper outputs and
+``Find_Bad_projections`` on seeded synthetic projection stacks narrower than 250
+detector columns (the reference's subsampling branch does not run on Python 3)
+and an explicit search radius (its default, ``min(Nx, Nz)/10``, calls NumPy's ``min``
+through ``from numpy import *`` and raises).
+Output: tests/golden/badproj.npz.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("GRAPTOR_REFERENCE", "/root/reference")
+
+
+def stacks():
+    rng = np.random.default_rng(20240607)
+    out = []
+    for NA, Nz, Nx in ((14, 40, 56), (11, 33, 48)):
+        base = np.zeros((Nz, Nx))
+        zz, xx = np.meshgrid(np.arange(Nz), np.arange(Nx), indexing="ij")
+        for _ in range(5):
+            cz, cx, r = rng.uniform(8, Nz - 8), rng.uniform(8, Nx - 8), rng.uniform(3, 9)
+            base += rng.uniform(0.5, 2.0) * ((zz - cz) ** 2 + (xx - cx) ** 2 < r * r)
+        data = np.stack([np.roll(base, int(rng.integers(-2, 3)), axis=1) for _ in range(NA)])
+        data += 0.05 * rng.random(data.shape)
+        for k in rng.choice(NA, 2, replace=False):  # two corrupted projections
+            data[k] = np.roll(data[k], 9, axis=0) + 0.8 * rng.random((Nz, Nx))
+        out.append(data)
+    return out
+
+
+def main():
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "refshim"))  # matplotlib stand-in
+    current = {}
+    h5 = types.ModuleType("h5utilities")
+    h5.Brightness_correction = lambda name, badname, cutedges, bad: (current["data"].copy(), None, 0)
+    sys.modules["h5utilities"] = h5
+    sys.modules["mrcfile"] = types.ModuleType("mrcfile")
+    misc = types.ModuleType("scipy.misc")
+    sys.modules["scipy.misc"] = misc
+    import scipy
+    scipy.misc = misc
+    sys.path.insert(0, REF)
+    import find_bad_ele as fb
+
+    res = {}
+    for n, data in enumerate(stacks()):
+        res[f"{n}/data"] = data
+        sm = fb.reduce_noise(data[0], 3)
+        res[f"{n}/reduce_noise0"] = sm
+        res[f"{n}/wgrad0"] = fb.weighted_gradient(sm)[1]
+        w1 = fb.weighted_gradient(fb.reduce_noise(data[1], 3))[1]
+        nrm, E = fb.compare_shift_twosided(res[f"{n}/wgrad0"], w1, 4)
+        res[f"{n}/shift_norm"] = np.array(nrm)
+        res[f"{n}/shift_E"] = E
+        for frac in (0.15, 3):
+            current["data"] = data
+            res[f"{n}/bad_{frac}"] = np.array(fb.Find_Bad_projections("stack", 4, frac))
+    np.savez_compressed(os.path.join(HERE, "badproj.npz"), **res)
+    print("wrote", os.path.join(HERE, "badproj.npz"), {k: v.shape for k, v in res.items() if "bad_" in k})
+
+
+if __name__ == "__main__":
+    main()

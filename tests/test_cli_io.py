@@ -1,0 +1,123 @@
+"""CPU tests of the command-line path: MRC / angle-file I/O, preprocessing, the
+option handling of the reference CLI, and the bad-projection detector against
+golden vectors produced by the reference's own find_bad_ele.py
+(tests/golden/make_badproj_golden.py)."""
+import os
+
+import numpy as np
+import pytest
+
+from graptor_gb300 import badproj, cli, mrc, preprocess
+
+
+def test_mrc_roundtrip_modes(tmp_path):
+    rng = np.random.default_rng(1)
+    for dt in (np.float32, np.int16, np.uint16, np.int8, np.float16):
+        a = (rng.standard_normal((3, 5, 7)) * 20).astype(dt)
+        p = str(tmp_path / f"a_{np.dtype(dt).name}.mrc")
+        mrc.write_mrc(p, a)
+        b = mrc.read_mrc(p)
+        assert b.dtype == np.dtype(dt) and np.array_equal(a, b)
+    # 2-D input is stored as one section; float64 as float32
+    p = str(tmp_path / "two.mrc")
+    mrc.write_mrc(p, rng.standard_normal((4, 6)))
+    assert mrc.read_mrc(p).shape == (1, 4, 6) and mrc.read_mrc(p).dtype == np.float32
+
+
+def test_mrc_big_endian_and_extended_header(tmp_path):
+    a = np.arange(2 * 3 * 4, dtype=np.float32).reshape(2, 3, 4)
+    head = np.zeros(256, ">i4")
+    head[0:4] = (4, 3, 2, 2)
+    head[23] = 64  # extended header bytes
+    b = bytearray(head.tobytes())
+    b[208:212] = b"MAP "
+    b[212:214] = b"\x11\x11"
+    p = str(tmp_path / "be.mrc")
+    with open(p, "wb") as fh:
+        fh.write(bytes(b) + b"\0" * 64 + a.astype(">f4").tobytes())
+    assert np.array_equal(mrc.read_mrc(p), a)
+
+
+def test_angle_files(tmp_path):
+    p = str(tmp_path / "s.mrc")
+    mrc.write_mrc(p, np.zeros((3, 2, 4), np.float32))
+    with pytest.raises(IOError):
+        mrc.read_angles(p)
+    with open(p.replace(".mrc", ".csv"), "w") as fh:
+        fh.write("-60,a\n0,b\n60,c\n")
+    assert np.allclose(mrc.read_angles(p), np.array([-60, 0, 60]) / 180 * np.pi)
+    with open(p.replace(".mrc", ".rawtlt"), "w") as fh:
+        fh.write("-30\n 0\n30\n")
+    assert np.allclose(mrc.read_angles(p), np.array([-30, 0, 30]) / 180 * np.pi)  # rawtlt wins
+    d, ang = mrc.read_projections(p)
+    assert d.dtype == np.float64 and d.shape == (3, 2, 4) and ang.size == 3
+
+
+def _stack(tmp_path, data, angles_deg, name="st"):
+    p = str(tmp_path / f"{name}.mrc")
+    mrc.write_mrc(p, data.astype(np.float32))
+    with open(p.replace(".mrc", ".rawtlt"), "w") as fh:
+        fh.write("\n".join(str(a) for a in angles_deg))
+    return p
+
+
+def test_brightness_correction_and_rescaling(tmp_path):
+    rng = np.random.default_rng(2)
+    data = rng.random((6, 5, 20)) + 1.0
+    p = _stack(tmp_path, data, np.linspace(-60, 60, 6))
+    data = data.astype(np.float32).astype(np.float64)
+    bad = [2, 5]  # 1-based
+    d, ang, _ = preprocess.brightness_correction(p, "", 0.1, bad)
+    keep = [0, 2, 3, 5]
+    ref = data[keep]
+    cut = 2
+    bg = 0.5 * (ref[:, :, 1:2].mean() + ref[:, :, 19:20].mean())
+    ref = ref[:, :, cut:20 - cut] - bg
+    m = ref.reshape(4, -1).mean(1)
+    ref = ref * (m.mean() / m)[:, None, None]
+    assert np.allclose(d, ref) and ang.size == 4
+    g, _, bgo = preprocess.global_rescaling(p, "", 0.1, bad)
+    r2 = data - data.min()
+    r2 = r2[keep]
+    r2 = r2 - r2.min()
+    assert np.isclose(bgo, 0.5 * (r2[:, :, 1:2].mean() + r2[:, :, 19:20].mean()))
+    assert np.allclose(g, r2[:, :, 2:18])
+    badfile = str(tmp_path / "bad.txt")
+    with open(badfile, "w") as fh:
+        fh.write("2\n")
+    d2, _, _ = preprocess.brightness_correction(p, badfile, 0.1, [5])
+    assert np.allclose(d2, d)
+
+
+def test_cli_option_handling(tmp_path):
+    assert cli.parse_method("frob3d") == ("Frobenius 3D Reconstruction", 1)
+    assert cli.parse_method("Uncorr2d") == ("Uncorrelated 2D Reconstruction", 0)
+    assert cli.parse_method("nucl3d") == ("Nuclear 3D Reconstruction", 1)
+    assert cli.parse_method("frobsubs")[1] == 2
+    assert cli.parse_method("whatever") == ("Frobenius 2D Reconstruction", 0)
+    p = _stack(tmp_path, np.ones((2, 2, 4)), [0, 10])
+    assert cli.resolve_names([p[:-4]]) == [p]
+    assert cli.resolve_names([p[:-4] + "."]) == [p]
+    with pytest.raises(IOError):
+        cli.resolve_names([str(tmp_path / "missing")])
+    a = cli.build_parser().parse_args([p])
+    assert a.Maxiter == 2000 and a.alpha == [4, 1.0] and a.Scalepars == [1, 98] and a.Overlapping == 1
+    with pytest.raises(ValueError):
+        cli.main([p, "--SliceLevels", "3", "1", "--Outfile", str(tmp_path / "o")])
+
+
+def test_bad_projections_match_reference(golden):
+    g = golden("badproj.npz")
+    for n in sorted({k.split("/")[0] for k in g}):
+        data = g[f"{n}/data"]
+        sm = badproj.reduce_noise(data[0], 3)
+        np.testing.assert_allclose(sm, g[f"{n}/reduce_noise0"], rtol=1e-13, atol=0)
+        w0 = badproj.weighted_gradient(sm)[1]
+        np.testing.assert_allclose(w0, g[f"{n}/wgrad0"], rtol=1e-13, atol=0)
+        w1 = badproj.weighted_gradient(badproj.reduce_noise(data[1], 3))[1]
+        nrm, E = badproj.compare_shift_twosided(w0, w1, 4)
+        np.testing.assert_allclose(E, g[f"{n}/shift_E"], rtol=1e-13, atol=0)
+        assert np.isclose(nrm, float(g[f"{n}/shift_norm"]), rtol=1e-12)
+        for frac in ("0.15", "3"):
+            got = badproj.find_bad_projections("stack", 4, float(frac) if "." in frac else int(frac), data=data)
+            assert list(got) == list(g[f"{n}/bad_{frac}"]), (n, frac)

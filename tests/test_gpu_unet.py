@@ -273,7 +273,7 @@ def test_unet_forward_backward_vs_float64():
     torch.cuda.synchronize()
     got_out, got_grad = out.cpu(), net.grad.cpu()
     report = {}
-    for emulate, tol_out, tol_grad in ((True, 1e-3, 5e-3), (False, 3e-2, 1e-1)):
+    for emulate, tol_out, tol_grad in ((True, 1e-3, 5e-3), (False, 5e-2, 3e-1)):
         ref, params = _ref_net(net, x.double(), emulate)
         names = [n for n, *_ in net.layers]
         leaves = [t for n in names for t in params[n]]
