@@ -8,6 +8,7 @@ Host arrays use the reference solver's layouts (see include/graptor_gb300.h).
 from __future__ import annotations
 
 import ctypes
+import math
 
 import numpy as np
 
@@ -162,10 +163,12 @@ class Problem:
                 "data": out[6], "fstar": out[7]}
 
     def solve_to_gap(self, tol: float = 1e-4, check_every: int = 50, max_iters: int = 100000) -> dict:
-        """Iterate until the relative gap is <= tol (checked every `check_every` iterations)."""
+        """Iterate until the relative gap is finite and <= tol (checked every
+        `check_every` iterations).  The gap is not finite while K u = 0 on a bin
+        with data (infinite KL primal value), e.g. before the first iteration."""
         done = 0
         g = self.gap()
-        while g["relative"] > tol and done < max_iters:
+        while not (math.isfinite(g["relative"]) and g["relative"] <= tol) and done < max_iters:
             n = min(check_every, max_iters - done)
             self.run(n)
             done += n
