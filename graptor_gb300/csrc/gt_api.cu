@@ -41,6 +41,7 @@ cudaError_t launch_ray_fill(const float4 *ofs, int N, int nd, int nang, const lo
                             cudaStream_t st);
 cudaError_t launch_bp_table(const float4 *ofs, int N, int nd, int nang, int2 *tab, cudaStream_t st);
 int num_proj_configs(int S, int which);
+bool dual_z2_ok(const IterParams &P, int tgv, int cpl);
 int gap_blocks(const IterParams &P);
 cudaError_t launch_gap_pass1(const IterParams &P, int disc, int tgv, int cpl, float *vt, double *part, int nb,
                              cudaStream_t st);
@@ -158,7 +159,7 @@ int capture(gt_problem *p, int n, cudaGraphExec_t *out) {
     return rc;
   }
   if (e != cudaSuccess) return cuda_err(e, "cudaStreamEndCapture", __LINE__);
-  e = cudaGraphInstantiate(out, g, 0);
+  e = cudaGraphInstantiate(out, g, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return cuda_err(e, "cudaGraphInstantiate", __LINE__);
   return GT_OK;
@@ -205,22 +206,24 @@ void set_scalars(gt_problem *p) {
 // the fastest; choices are cached per problem shape for the process lifetime.
 // It runs inside gt_set_data before the iterates are reset, so the extra
 // launches never touch the solve.
-using TuneKey = std::tuple<int, int, int, int, int, int, int>;
+using TuneKey = std::tuple<int, int, int, int, int, int, int, int, int, int>;
 std::mutex g_tune_mu;
-std::map<TuneKey, std::pair<int, int>> g_tune;
+std::map<TuneKey, std::tuple<int, int, int>> g_tune;
 
 int autotune(gt_problem *p) {
-  const int ncf = gt::num_proj_configs(p->d.S, 0), ncb = gt::num_proj_configs(p->d.S, 1);
+  const bool tgv = p->reg == GT_TGV;
+  const int nc[3] = {gt::num_proj_configs(p->d.S, 0), gt::num_proj_configs(p->d.S, 1),
+                     gt::dual_z2_ok(p->P, tgv, p->cpl) ? 2 : 1};
   p->P.fwd_cfg = 0;
   p->P.bp_cfg = 0;
-  if ((ncf <= 1 && ncb <= 1) || !p->autotune) return GT_OK;
-  const TuneKey key{p->d.dim, p->d.N, p->d.S, p->d.nd, p->d.nang, p->disc, p->d.C};
+  p->P.dual_cfg = 0;
+  if ((nc[0] <= 1 && nc[1] <= 1 && nc[2] <= 1) || !p->autotune) return GT_OK;
+  const TuneKey key{p->d.dim, p->d.N, p->d.S, p->d.nd, p->d.nang, p->disc, p->d.C, p->d.Nz, p->reg, p->cpl};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
     if (it != g_tune.end()) {
-      p->P.fwd_cfg = it->second.first;
-      p->P.bp_cfg = it->second.second;
+      std::tie(p->P.fwd_cfg, p->P.bp_cfg, p->P.dual_cfg) = it->second;
       return GT_OK;
     }
   }
@@ -228,21 +231,25 @@ int autotune(gt_problem *p) {
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   // configurations interleaved over several rounds; each keeps its fastest round
-  float ms_cfg[2][16];
+  float ms_cfg[3][16];
   for (auto &r : ms_cfg) for (float &v : r) v = 1e30f;
   int rc = GT_OK;
   const bool log = std::getenv("GRAPTOR_TUNE_LOG") != nullptr;
   for (int round = 0; round < 4 && rc == GT_OK; ++round) {
-    for (int which = 0; which < 2 && rc == GT_OK; ++which) {
-      const int nc = which == 0 ? ncf : ncb;
+    for (int which = 0; which < 3 && rc == GT_OK; ++which) {
+      if (nc[which] <= 1) continue;
       float best_ms = 1e30f;
-      for (int c = 0; c < nc; ++c) best_ms = std::min(best_ms, ms_cfg[which][c]);
-      for (int c = 0; c < nc && rc == GT_OK; ++c) {
+      for (int c = 0; c < nc[which]; ++c) best_ms = std::min(best_ms, ms_cfg[which][c]);
+      for (int c = 0; c < nc[which] && rc == GT_OK; ++c) {
         // after the first round only configurations within 30 % of the best are timed again
         if (round > 0 && ms_cfg[which][c] > 1.3f * best_ms) continue;
         gt::IterParams Q = p->P;
-        if (which == 0) Q.fwd_cfg = c; else Q.bp_cfg = c;
-        auto launch = [&]() { return which == 0 ? gt::launch_fwd(Q, p->disc, p->stream) : gt::launch_bp(Q, p->stream); };
+        if (which == 0) Q.fwd_cfg = c; else if (which == 1) Q.bp_cfg = c; else Q.dual_cfg = c;
+        auto launch = [&]() {
+          if (which == 0) return gt::launch_fwd(Q, p->disc, p->stream);
+          if (which == 1) return gt::launch_bp(Q, p->stream);
+          return gt::launch_dual(Q, tgv, p->cpl, p->stream);
+        };
         cudaError_t e = launch();  // warm-up
         if (e == cudaSuccess) e = cudaEventRecord(e0, p->stream);
         for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = launch();
@@ -255,22 +262,24 @@ int autotune(gt_problem *p) {
       }
     }
   }
-  int best[2] = {0, 0};
-  for (int which = 0; which < 2; ++which)
-    for (int c = 1; c < (which == 0 ? ncf : ncb); ++c)
+  int best[3] = {0, 0, 0};
+  static const char *names[3] = {"k_fwd", "k_bp", "k_dual"};
+  for (int which = 0; which < 3; ++which)
+    for (int c = 1; c < nc[which]; ++c)
       if (ms_cfg[which][c] < ms_cfg[which][best[which]]) best[which] = c;
   if (log && rc == GT_OK)
-    for (int which = 0; which < 2; ++which)
-      for (int c = 0; c < (which == 0 ? ncf : ncb); ++c)
-        fprintf(stderr, "graptor autotune %s cfg %d: %.4f ms%s\n", which ? "k_bp" : "k_fwd", c, ms_cfg[which][c],
+    for (int which = 0; which < 3; ++which)
+      for (int c = 0; c < nc[which] && nc[which] > 1; ++c)
+        fprintf(stderr, "graptor autotune %s cfg %d: %.4f ms%s\n", names[which], c, ms_cfg[which][c],
                 c == best[which] ? " *" : "");
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
   p->P.fwd_cfg = best[0];
   p->P.bp_cfg = best[1];
+  p->P.dual_cfg = best[2];
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune[key] = {best[0], best[1]};
+  g_tune[key] = std::make_tuple(best[0], best[1], best[2]);
   return GT_OK;
 }
 
@@ -336,7 +345,15 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
     p->own_stream = true;
   }
   {
-    cudaError_t e1 = cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking);
+    // The projector chain is the iteration's critical path (k_fwd -> k_bp ->
+    // k_update) while k_dual beside it has slack, so the side stream gets the
+    // highest priority: its blocks are scheduled first when both compete for SMs.
+    // GRAPTOR_SIDE_PRIORITY=0 keeps the default priority.
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    const char *env = std::getenv("GRAPTOR_SIDE_PRIORITY");
+    const int prio = (env && env[0] == '0') ? lo : hi;
+    cudaError_t e1 = cudaStreamCreateWithPriority(&p->side, cudaStreamNonBlocking, prio);
     if (e1 == cudaSuccess) e1 = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
     if (e1 == cudaSuccess) e1 = cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming);
     if (e1 != cudaSuccess) return fail(cuda_err(e1, "stream/event setup", __LINE__));
@@ -625,6 +642,20 @@ int gt_set_tuning(gt_problem *p, int fwd_cfg, int bp_cfg) {
   return GT_OK;
 }
 
+int gt_set_dual_shape(gt_problem *p, int cfg) {
+  if (!p) return set_err(GT_ERR_ARG, "null argument");
+  const int n = gt::dual_z2_ok(p->P, p->reg == GT_TGV, p->cpl) ? 2 : 1;
+  if (cfg < 0 || cfg >= n) return set_err(GT_ERR_ARG, "dual launch shape %d out of range (%d available)", cfg, n);
+  CK(cudaSetDevice(p->device));
+  CK(cudaStreamSynchronize(p->stream));
+  p->P.dual_cfg = cfg;
+  if (p->g_one) { cudaGraphExecDestroy(p->g_one); p->g_one = nullptr; }
+  if (p->g_chunk) { cudaGraphExecDestroy(p->g_chunk); p->g_chunk = nullptr; }
+  return GT_OK;
+}
+
+int gt_get_dual_shape(gt_problem *p) { return p ? p->P.dual_cfg : -1; }
+
 int gt_get_tuning(gt_problem *p, int out[2]) {
   if (!p || !out) return set_err(GT_ERR_ARG, "null argument");
   out[0] = p->P.fwd_cfg;
@@ -797,7 +828,7 @@ static int batch_capture(gt_batch *b, int n, cudaGraphExec_t *out) {
     if (rc) return rc;
     return cuda_err(e != cudaSuccess ? e : e2, "batch capture", __LINE__);
   }
-  e = cudaGraphInstantiate(out, g, 0);
+  e = cudaGraphInstantiate(out, g, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return cuda_err(e, "cudaGraphInstantiate (batch)", __LINE__);
   return GT_OK;

@@ -42,6 +42,7 @@ struct IterParams {
   float stepsize;
   int cbase;             // first channel handled by a k_dual launch (0 unless C > 8)
   int fwd_cfg, bp_cfg;   // projector launch shapes (see launch_fwd / launch_bp)
+  int dual_cfg;          // 0: k_dual, 1: k_dual_z2 (where dual_z2_ok)
   const float4 *ofs;     // [nang] (X, Y, offset, Xinv)
   const long long *ray_start;  // [nd*nang + 1] ray table offsets (null: walk rays on the fly)
   const int2 *ray_ent;         // (pixel, weight bits) entries of all rays

@@ -387,6 +387,172 @@ __global__ void __launch_bounds__(256) k_dual(const IterParams P) {
   }
 }
 
+// k_dual_z2: k_dual for 3-D TGV with Frobenius or uncorrelated coupling, a thread
+// per (pixel, pair of consecutive slices z0, z0+1): every field is read and
+// written as float2 (half the load instructions of k_dual), in two phases (v,
+// then w) to bound the registers.  Every value is computed by the same
+// operations as in k_dual, so the iterates are bit-identical.  Needs Nz even.
+__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ void st2(float *p, float a, float b) { *reinterpret_cast<float2 *>(p) = make_float2(a, b); }
+
+template <int CPL, int CMAX>
+__global__ void __launch_bounds__(256) k_dual_z2(const IterParams P) {
+  const Dims d = P.d;
+  const int nzq = d.Nz >> 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)d.N * d.N * nzq) return;
+  const int pix = (int)(t / nzq);
+  const int z0 = 2 * (int)(t - (long long)pix * nzq);
+  const int y = pix / d.N, x = pix - y * d.N;
+  const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
+  const float sigma = P.sigma;
+  const float *__restrict__ ub = P.ubar;
+  const float *__restrict__ pb = P.pbar;
+  const int nC = min(CMAX, d.C);
+  const bool hx = x < d.N - 1, hy = y < d.N - 1, hz = z0 + 1 < d.Nz - 1;  // forward neighbours
+  const bool lx = x > 0, ly = y > 0, lz = z0 > 0;                          // backward neighbours
+
+  // ---- v: gradient of ubar minus pbar, ball projection, store
+  {
+    float vv[CMAX][3][2];
+#pragma unroll
+    for (int c = 0; c < CMAX; ++c) {
+      if (c >= nC) break;
+      const size_t i = (size_t)pix * S + (size_t)c * d.Nz + z0;
+      const float2 u = ld2(ub + i);
+      float g[3][2];
+      const float mu0 = -u.x, mu1 = -u.y;
+      if (hx) { const float2 n = ld2(ub + i + S); g[0][0] = mu0 + n.x; g[0][1] = mu1 + n.y; } else { g[0][0] = g[0][1] = 0.f; }
+      if (hy) { const float2 n = ld2(ub + i + rowS); g[1][0] = mu0 + n.x; g[1][1] = mu1 + n.y; } else { g[1][0] = g[1][1] = 0.f; }
+      g[2][0] = (mu0 + u.y) / P.stepsize;
+      g[2][1] = (hz ? mu1 + ub[i + 2] : 0.f) / P.stepsize;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float2 pc = ld2(pb + k * vol + i), v = ld2(P.v + k * vol + i);
+        vv[c][k][0] = v.x + sigma * (g[k][0] - pc.x);
+        vv[c][k][1] = v.y + sigma * (g[k][1] - pc.y);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (CPL == FROB) {
+        float n2 = 0.f;
+#pragma unroll
+        for (int c = 0; c < CMAX; ++c) {
+          if (c >= nC) break;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) n2 += vv[c][k][q] * vv[c][k][q];
+        }
+        const float nv = sqrtf(n2) * P.ainv1;
+        if (nv > 1.f) {
+#pragma unroll
+          for (int c = 0; c < CMAX; ++c) {
+            if (c >= nC) break;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) vv[c][k][q] = vv[c][k][q] / nv;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < CMAX; ++c) {
+          if (c >= nC) break;
+          float n2 = 0.f;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) n2 += vv[c][k][q] * vv[c][k][q];
+          const float nv = sqrtf(n2) * P.ainv1;
+          if (nv > 1.f) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) vv[c][k][q] = vv[c][k][q] / nv;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < CMAX; ++c) {
+      if (c >= nC) break;
+      const size_t i = (size_t)pix * S + (size_t)c * d.Nz + z0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) st2(P.v + k * vol + i, vv[c][k][0], vv[c][k][1]);
+    }
+  }
+
+  // ---- w: symmetrised gradient of pbar, ball projection, store
+  float ww[CMAX][6][2];
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c) {
+    if (c >= nC) break;
+    const size_t i = (size_t)pix * S + (size_t)c * d.Nz + z0;
+    float a[3][2], b[3][2], cz[3][2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float2 pc = ld2(pb + k * vol + i);
+      if (lx) { const float2 n = ld2(pb + k * vol + i - S); a[k][0] = pc.x - n.x; a[k][1] = pc.y - n.y; } else { a[k][0] = a[k][1] = 0.f; }
+      if (ly) { const float2 n = ld2(pb + k * vol + i - rowS); b[k][0] = pc.x - n.x; b[k][1] = pc.y - n.y; } else { b[k][0] = b[k][1] = 0.f; }
+      cz[k][0] = (lz ? pc.x - pb[k * vol + i - 1] : 0.f) / P.stepsize;
+      cz[k][1] = (pc.y - pc.x) / P.stepsize;
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      float e[6];
+      e[0] = a[0][q]; e[1] = b[1][q]; e[2] = cz[2][q];
+      e[3] = 0.5f * (a[1][q] + b[0][q]);
+      e[4] = 0.5f * (a[2][q] + cz[0][q]);
+      e[5] = 0.5f * (b[2][q] + cz[1][q]);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) ww[c][k][q] = e[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float2 w = ld2(P.w + k * vol + i);
+      ww[c][k][0] = w.x + sigma * ww[c][k][0];
+      ww[c][k][1] = w.y + sigma * ww[c][k][1];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    if (CPL == FROB) {
+      float n2 = 0.f;
+#pragma unroll
+      for (int c = 0; c < CMAX; ++c) {
+        if (c >= nC) break;
+        float wc[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) wc[k] = ww[c][k][q];
+        n2 += wnorm2<3, FROB>(wc);
+      }
+      const float nw = sqrtf(n2) * P.ainv0;
+      if (nw > 1.f) {
+#pragma unroll
+        for (int c = 0; c < CMAX; ++c) {
+          if (c >= nC) break;
+#pragma unroll
+          for (int k = 0; k < 6; ++k) ww[c][k][q] = ww[c][k][q] / nw;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < CMAX; ++c) {
+        if (c >= nC) break;
+        float wc[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) wc[k] = ww[c][k][q];
+        const float nw = sqrtf(wnorm2<3, UNCORR>(wc)) * P.ainv0;
+        if (nw > 1.f) {
+#pragma unroll
+          for (int k = 0; k < 6; ++k) ww[c][k][q] = ww[c][k][q] / nw;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c) {
+    if (c >= nC) break;
+    const size_t i = (size_t)pix * S + (size_t)c * d.Nz + z0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) st2(P.w + k * vol + i, ww[c][k][0], ww[c][k][1]);
+  }
+}
+
 // coherent vector loads / stores of UW consecutive slices (fields a kernel also writes)
 template <int VW> __device__ __forceinline__ void ldw(const float *p, float (&r)[VW]) {
   if (VW == 4) {
@@ -1134,7 +1300,9 @@ __global__ void k_feasible(float *__restrict__ f, const float *__restrict__ r1, 
 // Data dual consistent with a primal image: lambda at the fixed point of the
 // lambda update for the given K u.  KL (update_lambda_KL, 3-D :690-704): the
 // fixed point of lam = s - (s - mu + sqrt((s - mu)^2 + 4 sigma f mu)) / 2 with
-// s = lam + sigma ku is lam = mu (1 - f / ku); where ku <= 0 lambda is kept.
+// s = lam + sigma ku is lam = mu (1 - f / ku).  Where K u is zero or far below
+// the data (f > 10 K u: the image misses counts there) that value is unbounded
+// below and would throw the next primal step far off, so lambda is kept.
 // L2 (update_lambda_L2, :677-688, weight m = mu / (sigma + mu)): lam = mu (ku - f).
 __global__ void k_lambda_fixed(float *__restrict__ lam, const float *__restrict__ ku, const float *__restrict__ f,
                                const double *__restrict__ mu, long long nbin, int S, int Nz, int disc) {
@@ -1143,7 +1311,7 @@ __global__ void k_lambda_fixed(float *__restrict__ lam, const float *__restrict_
   const int s = (int)(t % S);
   const float m = (float)mu[s / Nz], k = ku[t], fv = f[t];
   if (disc == 0) {
-    if (k > 0.f) lam[t] = m * (1.0f - fv / k);
+    if (k > 0.f && fv <= 10.f * k) lam[t] = m * (1.0f - fv / k);
   } else {
     lam[t] = m * (k - fv);
   }
@@ -1468,11 +1636,29 @@ __global__ void __launch_bounds__(256) k_gap_box(const IterParams P, const float
 // ===========================================================================
 static inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// k_dual_z2 applies: 3-D TGV, Frobenius or uncorrelated coupling, C <= 4, Nz even
+bool dual_z2_ok(const IterParams &P, int tgv, int cpl) {
+  return P.d.dim == 3 && tgv && (cpl == FROB || cpl == UNCORR) && P.d.C <= 4 && P.d.Nz % 2 == 0;
+}
+
+template <int CPL>
+static void launch_dual_z2(const IterParams &P, cudaStream_t st) {
+  const unsigned g = blocks_for((long long)P.d.N * P.d.N * (P.d.Nz / 2), 256);
+  const int C = P.d.C;
+  if (C <= 1) k_dual_z2<CPL, 1><<<g, 256, 0, st>>>(P);
+  else if (C <= 2) k_dual_z2<CPL, 2><<<g, 256, 0, st>>>(P);
+  else k_dual_z2<CPL, 4><<<g, 256, 0, st>>>(P);
+}
+
 template <int DIM, bool TGV, int CPL>
 static cudaError_t launch_dual_c(const IterParams &P, cudaStream_t st) {
   const long long n = (long long)P.d.N * P.d.N * P.d.Nz;
   const unsigned g = blocks_for(n, 256);
   const int C = P.d.C;
+  if (DIM == 3 && TGV && CPL != NUCL && P.dual_cfg == 1 && C <= 4 && P.d.Nz % 2 == 0) {
+    launch_dual_z2<CPL == NUCL ? FROB : CPL>(P, st);
+    return cudaGetLastError();
+  }
   if (C <= 1) k_dual<DIM, TGV, CPL, 1><<<g, 256, 0, st>>>(P);
   else if (C <= 2) k_dual<DIM, TGV, CPL, 2><<<g, 256, 0, st>>>(P);
   else if (C <= 4) k_dual<DIM, TGV, CPL, 4><<<g, 256, 0, st>>>(P);

@@ -137,6 +137,11 @@ class Problem:
         L.check(L.lib().gt_set_tuning(self._h, int(fwd), int(bp)))
         return self
 
+    def set_dual_shape(self, cfg: int):
+        """Force the dual kernel's launch shape (see gt_set_dual_shape)."""
+        L.check(L.lib().gt_set_dual_shape(self._h, int(cfg)))
+        return self
+
     def dual_from_primal(self):
         """Set lambda consistent with the current u (for warm starts)."""
         L.check(L.lib().gt_dual_from_primal(self._h))
@@ -153,7 +158,7 @@ class Problem:
         """Projector launch shapes the autotuner chose (see launch_fwd / launch_bp)."""
         out = (ctypes.c_int * 2)()
         L.check(L.lib().gt_get_tuning(self._h, out))
-        return {"fwd_cfg": out[0], "bp_cfg": out[1]}
+        return {"fwd_cfg": out[0], "bp_cfg": out[1], "dual_cfg": L.lib().gt_get_dual_shape(self._h)}
 
     def gap(self, U: float = 0.0) -> dict:
         """FP64 primal-dual gap of the current iterate on the box u in [0, U] (U <= 0: 2 max u)."""

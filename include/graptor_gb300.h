@@ -104,6 +104,12 @@ GT_API int gt_get_tuning(gt_problem *p, int out[2]);
 /* Force the projector launch shapes (for tests and measurements); the values
  * range over the configurations listed at launch_fwd / launch_bp. */
 GT_API int gt_set_tuning(gt_problem *p, int fwd_cfg, int bp_cfg);
+/* Launch shape of the dual kernel: 0 = one slice per thread (every case),
+ * 1 = two slices per thread with float2 accesses (3-D TGV, Frobenius or
+ * uncorrelated coupling, C <= 4, Nz even).  Both give bit-identical iterates;
+ * the autotuner picks the faster.  gt_get_dual_shape returns the current one. */
+GT_API int gt_set_dual_shape(gt_problem *p, int cfg);
+GT_API int gt_get_dual_shape(gt_problem *p);
 
 /* Scalars the run uses: [0] normest, [1] sigma, [2] tau, [3] iterations run. */
 GT_API int gt_get_scalars(gt_problem *p, double out[4]);
@@ -239,7 +245,7 @@ GT_API int gt_get_state_device(gt_problem *p, int field, float *dev);
 GT_API int gt_set_state_device(gt_problem *p, int field, const float *dev);
 /* Set the data dual lambda to the value consistent with the current u: the fixed
  * point of the reference's lambda update for K u (KL: mu (1 - f / K u), kept
- * where K u <= 0; L2: mu (K u - f)).  For warm starts (set u, then this).  No
+ * where f > 10 K u, K u = 0 included; L2: mu (K u - f)).  For warm starts (set u, then this).  No
  * counterpart in the reference, which starts lambda at zero. */
 GT_API int gt_dual_from_primal(gt_problem *p);
 /* The problem's CUDA stream (the one gt_desc.stream named, or its own). */
