@@ -406,6 +406,83 @@ def run_batched(args, rank, world, local):
             "speedup_vs_fixed_shape": out["fixed_shape"]["seconds"] / best["seconds"]}
 
 
+WARM = dict(N=128, Nz=32, C=2, nang=71, pre=500, tol=1e-2, check_every=100, max_iters=40000,
+            weights=os.path.join(ROOT, "graptor_gb300", "weights", "unet_tgv_kl_c2_p500.npz"))
+
+
+def run_warmstart(args, rank, world, local):
+    """Time to relative primal-dual gap <= tol on held-out seeded problems
+    (3-D TGV-KL, FROB, 2 channels, 128^2 x 32, 71 angles): the plain solver
+    cold-started, problems one after another, against the learned warm start
+    (pre cold iterations, U-Net prediction of u, lambda from K u) with all
+    problems advanced together as one Batch.  Set-up (buffers, data upload,
+    operator norm, autotuning) is outside both timed regions; gap checks every
+    check_every iterations are inside both."""
+    import math
+
+    import torch
+
+    from graptor_gb300 import warmstart as WS
+    from graptor_gb300.solver import Batch, Problem
+    torch.cuda.set_device(local)
+    N, Nz, C, tol = WARM["N"], WARM["Nz"], WARM["C"], WARM["tol"]
+    seeds = [9000 + 1000 * rank + k for k in range(args.seeds)]
+    cases = [WS.phantom_case(s, N, Nz, C, WARM["nang"], device=local) for s in seeds]
+    specs = [WS.problem_spec(N, Nz, C, ang) for _, ang in cases]
+    net = WS.UNet3D.load(args.weights or WARM["weights"], device=local)
+
+    def done(g):
+        return math.isfinite(g) and g <= tol
+
+    # plain cold start, one problem after another
+    cold_its, cold_s, lpi = [], 0.0, 4
+    for (f, _), sp in zip(cases, specs):
+        with Problem(**sp, device=local) as p:
+            p.set_data(f).synchronize()
+            lpi = p.launches_per_iteration
+            t0 = time.perf_counter()
+            it, g = WS.iterations_to_gap(p, tol, WARM["check_every"], WARM["max_iters"])
+            p.synchronize()
+            cold_s += time.perf_counter() - t0
+            cold_its.append(it)
+    # warm start + batch
+    warm_its = [None] * len(cases)
+    with Batch(specs, device=local) as b:
+        for k, (f, _) in enumerate(cases):
+            b[k].set_data(f)
+        b.invalidate()
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        b.run(WARM["pre"]).synchronize()
+        ws = WS.WarmStarter(net, ("u",), pre_iters=0)
+        for k, (f, _) in enumerate(cases):
+            ws.apply(b[k], f)
+        its = WARM["pre"]
+        while any(w is None for w in warm_its) and its < WARM["max_iters"]:
+            b.run(WARM["check_every"])
+            its += WARM["check_every"]
+            for k in range(len(cases)):
+                if warm_its[k] is None and done(b[k].gap()["relative"]):
+                    warm_its[k] = its
+        b.synchronize()
+        warm_s = time.perf_counter() - t0
+    cold_s = max_over_ranks(cold_s, world)
+    warm_s = max_over_ranks(warm_s, world)
+    if rank != 0:
+        return None
+    return {"metric": "time-to-gap", "value": warm_s, "unit": "s", "n_gpus": world, "steps": len(cases),
+            "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 2-channel ellipsoid phantoms, Poisson peaks 1e4 / 20)",
+            "config": {"workload": f"time to relative gap <= {tol}: {len(cases)} held-out 3D TGV-KL FROB problems "
+                                   f"{N}x{N}x{Nz}, {C} channels, {WARM['nang']} angles",
+                       "pre_iterations": WARM["pre"], "check_every": WARM["check_every"],
+                       "weights": os.path.relpath(args.weights or WARM["weights"], ROOT)},
+            "cold_seconds": cold_s, "warm_batched_seconds": warm_s, "speedup": cold_s / warm_s,
+            "cold_iterations": cold_its, "warm_iterations": warm_its,
+            "gpu_launches": lpi * (sum(cold_its) + len(cases) * its)}
+
+
 def ncu_traffic(kernel):
     """DRAM bytes per launch of `kernel` from the committed ncu summary, if present."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
@@ -431,9 +508,12 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="image side (default 256); profiler captures")
     ap.add_argument("--nang", type=int, default=None,
                     help="projection angles (default 71; the 768^2 x 384 large run uses 141)")
-    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched"],
-                    help="coupled3d: the 3-D 4-channel workload (default); batched: 64 uneven problems")
+    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart"],
+                    help="coupled3d: the 3-D 4-channel workload (default); batched: 64 uneven problems; "
+                         "warmstart: time to gap, cold start against learned warm start + batch")
     ap.add_argument("--batch", type=int, default=64, help="problems per rank for --workload batched")
+    ap.add_argument("--seeds", type=int, default=8, help="held-out problems per rank for --workload warmstart")
+    ap.add_argument("--weights", default=None, help="network weights for --workload warmstart")
     ap.add_argument("--quick", action="store_true",
                     help="only the device-timed region (no e2e, kernel timing or CPU baseline): profiler runs")
     args = ap.parse_args()
@@ -448,6 +528,8 @@ def main():
         out = run_reference(args, rank, world)
     elif args.workload == "batched":
         out = run_batched(args, rank, world, local)
+    elif args.workload == "warmstart":
+        out = run_warmstart(args, rank, world, local)
     else:
         from oracle import oracle as O
         O.build()  # the CPU-baseline leg needs the oracle library (built before any GPU work)

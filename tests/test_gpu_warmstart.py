@@ -1,0 +1,42 @@
+"""What the learned warm start gains, on held-out problems.
+
+The committed network (graptor_gb300/weights/unet_tgv_kl_c2_p500.npz, trained by
+``python -m graptor_gb300.warmstart train`` on solver-generated pairs) takes u
+after 500 cold iterations of a 3-D TGV-KL, FROB-coupled, 2-channel 128^2 x 32
+problem and predicts the converged u; lambda is then set from K u.  The tests
+count iterations to relative gap 1e-2 (the library's FP64 gap) against the
+cold-started plain solver on seeds the network never saw, check that the warm
+start ends at the cold run's minimiser, and that the network adds to what the
+lambda reset alone gives.
+"""
+import os
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+WEIGHTS = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "graptor_gb300", "weights",
+                       "unet_tgv_kl_c2_p500.npz")
+
+
+@pytest.fixture(scope="module")
+def rows():
+    from graptor_gb300 import warmstart as W
+    net = W.UNet3D.load(WEIGHTS)
+    r = W.evaluate(net, (9100, 9101), 128, 32, 2, fields=("u",), pre_iters=500, tol=1e-2, log=print)
+    return r
+
+
+def test_warm_start_reaches_the_gap_sooner(rows):
+    for r in rows:
+        assert r["warm"]["gap"] <= 1e-2, r
+        assert 1.5 * r["warm"]["iterations"] <= r["cold"]["iterations"], r
+
+
+def test_warm_start_converges_to_the_same_minimiser(rows):
+    for r in rows:
+        assert r["warm"]["distance_to_cold"] < 0.05, r
+
+
+def test_network_adds_to_the_dual_reset(rows):
+    assert sum(r["warm"]["iterations"] for r in rows) < sum(r["reset"]["iterations"] for r in rows), rows
