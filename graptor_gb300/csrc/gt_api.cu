@@ -31,7 +31,7 @@ cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, in
 cudaError_t launch_transpose(const float *in, float *out, int rows, int cols, cudaStream_t st);
 cudaError_t launch_feasible(float *f, const float *r1, int nbin1, int S, cudaStream_t st);
 cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
-                                int Nz, int disc, cudaStream_t st);
+                                int Nz, int disc, int keep_empty, cudaStream_t st);
 cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, double *d_img, double *d_sino,
                       double *d_part, double *out, cudaStream_t st);
 cudaError_t fill_f64(double *x, size_t n, double v, cudaStream_t st);
@@ -613,16 +613,19 @@ int gt_set_state_device(gt_problem *p, int field, const float *dev) {
   return GT_OK;
 }
 
-int gt_dual_from_primal(gt_problem *p) {
+int gt_dual_from_primal_ex(gt_problem *p, int flags) {
   if (!p) return set_err(GT_ERR_ARG, "null argument");
   if (!p->has_data) return set_err(GT_ERR_STATE, "gt_dual_from_primal before gt_set_data");
+  if (flags & ~GT_DUAL_KEEP_EMPTY) return set_err(GT_ERR_ARG, "unknown flags %d", flags);
   CK(cudaSetDevice(p->device));
   // K u into the ku buffer (the next iteration's forward projection overwrites it)
   CK(gt::launch_radon(p->u, p->ku, p->ofs, p->d.N, p->d.nd, p->d.nang, p->d.S, p->stream));
   CK(gt::launch_lambda_fixed(p->lam, p->ku, p->f, p->mu64, (long long)p->d.nd * p->d.nang, p->d.S, p->d.Nz, p->disc,
-                             p->stream));
+                             (flags & GT_DUAL_KEEP_EMPTY) ? 1 : 0, p->stream));
   return GT_OK;
 }
+
+int gt_dual_from_primal(gt_problem *p) { return gt_dual_from_primal_ex(p, 0); }
 
 void *gt_problem_stream(gt_problem *p) { return p ? (void *)p->stream : nullptr; }
 

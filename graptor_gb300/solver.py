@@ -142,9 +142,10 @@ class Problem:
         L.check(L.lib().gt_set_dual_shape(self._h, int(cfg)))
         return self
 
-    def dual_from_primal(self):
-        """Set lambda consistent with the current u (for warm starts)."""
-        L.check(L.lib().gt_dual_from_primal(self._h))
+    def dual_from_primal(self, keep_empty: bool = False):
+        """Set lambda consistent with the current u (for warm starts); with
+        keep_empty, bins without data keep their lambda."""
+        L.check(L.lib().gt_dual_from_primal_ex(self._h, 1 if keep_empty else 0))
         return self
 
     @property

@@ -335,10 +335,12 @@ class WarmStarter:
     fixed point of its update for the predicted u (gt_dual_from_primal): without
     that the first iterations pull u back towards the cold-start state."""
 
-    def __init__(self, net: UNet3D, fields=("u", "v"), pre_iters: int = 20, use=None, reset_dual: bool = True):
+    def __init__(self, net: UNet3D, fields=("u", "v"), pre_iters: int = 20, use=None, reset_dual: bool = True,
+                 keep_empty: bool = False):
         self.net, self.fields, self.pre_iters = net, tuple(fields), int(pre_iters)
         self.use = tuple(use) if use is not None else self.fields  # predicted fields written to the solver
         self.reset_dual = bool(reset_dual)
+        self.keep_empty = bool(keep_empty)  # leave lambda on bins without data
         if self.fields[0] != "u":
             raise ValueError("the first predicted field must be u (the residual channels)")
 
@@ -396,7 +398,7 @@ class WarmStarter:
             ch += n
         # the data dual consistent with the predicted image (fixed point of its update)
         if self.reset_dual:
-            _ck(lib.gt_dual_from_primal(prob._h))
+            _ck(lib.gt_dual_from_primal_ex(prob._h, 1 if self.keep_empty else 0))
         prob.synchronize()
         return prob
 

@@ -248,6 +248,10 @@ GT_API int gt_set_state_device(gt_problem *p, int field, const float *dev);
  * where f > 10 K u, K u = 0 included; L2: mu (K u - f)).  For warm starts (set u, then this).  No
  * counterpart in the reference, which starts lambda at zero. */
 GT_API int gt_dual_from_primal(gt_problem *p);
+/* gt_dual_from_primal with flags: GT_DUAL_KEEP_EMPTY leaves lambda unchanged on
+ * bins without data (f = 0), where the fixed point is mu itself. */
+enum { GT_DUAL_KEEP_EMPTY = 1 };
+GT_API int gt_dual_from_primal_ex(gt_problem *p, int flags);
 /* The problem's CUDA stream (the one gt_desc.stream named, or its own). */
 GT_API void *gt_problem_stream(gt_problem *p);
 
