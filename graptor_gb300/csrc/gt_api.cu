@@ -31,7 +31,7 @@ cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, in
 cudaError_t launch_transpose(const float *in, float *out, int rows, int cols, cudaStream_t st);
 cudaError_t launch_feasible(float *f, const float *r1, int nbin1, int S, cudaStream_t st);
 cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
-                                int Nz, int disc, int keep_empty, cudaStream_t st);
+                                int Nz, int disc, int keep_empty, float cap, cudaStream_t st);
 cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, double *d_img, double *d_sino,
                       double *d_part, double *out, cudaStream_t st);
 cudaError_t fill_f64(double *x, size_t n, double v, cudaStream_t st);
@@ -616,12 +616,13 @@ int gt_set_state_device(gt_problem *p, int field, const float *dev) {
 int gt_dual_from_primal_ex(gt_problem *p, int flags) {
   if (!p) return set_err(GT_ERR_ARG, "null argument");
   if (!p->has_data) return set_err(GT_ERR_STATE, "gt_dual_from_primal before gt_set_data");
-  if (flags & ~GT_DUAL_KEEP_EMPTY) return set_err(GT_ERR_ARG, "unknown flags %d", flags);
+  if (flags & ~(GT_DUAL_KEEP_EMPTY | GT_DUAL_CAP10 | GT_DUAL_CAP100)) return set_err(GT_ERR_ARG, "unknown flags %d", flags);
+  const float cap = (flags & GT_DUAL_CAP100) ? 100.f : ((flags & GT_DUAL_CAP10) ? 10.f : 0.f);
   CK(cudaSetDevice(p->device));
   // K u into the ku buffer (the next iteration's forward projection overwrites it)
   CK(gt::launch_radon(p->u, p->ku, p->ofs, p->d.N, p->d.nd, p->d.nang, p->d.S, p->stream));
   CK(gt::launch_lambda_fixed(p->lam, p->ku, p->f, p->mu64, (long long)p->d.nd * p->d.nang, p->d.S, p->d.Nz, p->disc,
-                             (flags & GT_DUAL_KEEP_EMPTY) ? 1 : 0, p->stream));
+                             (flags & GT_DUAL_KEEP_EMPTY) ? 1 : 0, cap, p->stream));
   return GT_OK;
 }
 

@@ -1305,7 +1305,8 @@ __global__ void k_feasible(float *__restrict__ f, const float *__restrict__ r1, 
 // below and would throw the next primal step far off, so lambda is kept.
 // L2 (update_lambda_L2, :677-688, weight m = mu / (sigma + mu)): lam = mu (ku - f).
 __global__ void k_lambda_fixed(float *__restrict__ lam, const float *__restrict__ ku, const float *__restrict__ f,
-                               const double *__restrict__ mu, long long nbin, int S, int Nz, int disc, int keep_empty) {
+                               const double *__restrict__ mu, long long nbin, int S, int Nz, int disc, int keep_empty,
+                               float cap) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nbin * S) return;
   const int s = (int)(t % S);
@@ -1313,14 +1314,16 @@ __global__ void k_lambda_fixed(float *__restrict__ lam, const float *__restrict_
   if (keep_empty && fv == 0.f) return;
   if (disc == 0) {
     if (k > 0.f && fv <= 10.f * k) lam[t] = m * (1.0f - fv / k);
+    else if (cap > 0.f && fv > 0.f) lam[t] = m * (1.0f - cap);  // f / K u capped: a strong push up the ray
   } else {
     lam[t] = m * (k - fv);
   }
 }
 
 cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
-                                int Nz, int disc, int keep_empty, cudaStream_t st) {
-  k_lambda_fixed<<<(unsigned)((nbin * S + 255) / 256), 256, 0, st>>>(lam, ku, f, mu, nbin, S, Nz, disc, keep_empty);
+                                int Nz, int disc, int keep_empty, float cap, cudaStream_t st) {
+  k_lambda_fixed<<<(unsigned)((nbin * S + 255) / 256), 256, 0, st>>>(lam, ku, f, mu, nbin, S, Nz, disc, keep_empty,
+                                                                      cap);
   return cudaGetLastError();
 }
 

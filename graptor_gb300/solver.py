@@ -142,10 +142,12 @@ class Problem:
         L.check(L.lib().gt_set_dual_shape(self._h, int(cfg)))
         return self
 
-    def dual_from_primal(self, keep_empty: bool = False):
+    def dual_from_primal(self, keep_empty: bool = False, cap: int = 0):
         """Set lambda consistent with the current u (for warm starts); with
-        keep_empty, bins without data keep their lambda."""
-        L.check(L.lib().gt_dual_from_primal_ex(self._h, 1 if keep_empty else 0))
+        keep_empty, bins without data keep their lambda; cap 10 or 100 sets
+        lambda = mu (1 - cap) where f > 10 K u (see gt_dual_from_primal_ex)."""
+        flags = (1 if keep_empty else 0) | {0: 0, 10: 2, 100: 4}[int(cap)]
+        L.check(L.lib().gt_dual_from_primal_ex(self._h, flags))
         return self
 
     @property

@@ -336,11 +336,12 @@ class WarmStarter:
     that the first iterations pull u back towards the cold-start state."""
 
     def __init__(self, net: UNet3D, fields=("u", "v"), pre_iters: int = 20, use=None, reset_dual: bool = True,
-                 keep_empty: bool = False):
+                 keep_empty: bool = False, cap: int = 0):
         self.net, self.fields, self.pre_iters = net, tuple(fields), int(pre_iters)
         self.use = tuple(use) if use is not None else self.fields  # predicted fields written to the solver
         self.reset_dual = bool(reset_dual)
         self.keep_empty = bool(keep_empty)  # leave lambda on bins without data
+        self.cap = int(cap)  # 0: keep lambda where f > 10 K u; 10 / 100: lambda = mu (1 - cap) there
         if self.fields[0] != "u":
             raise ValueError("the first predicted field must be u (the residual channels)")
 
@@ -398,7 +399,7 @@ class WarmStarter:
             ch += n
         # the data dual consistent with the predicted image (fixed point of its update)
         if self.reset_dual:
-            _ck(lib.gt_dual_from_primal_ex(prob._h, 1 if self.keep_empty else 0))
+            _ck(lib.gt_dual_from_primal_ex(prob._h, (1 if self.keep_empty else 0) | {0: 0, 10: 2, 100: 4}[self.cap]))
         prob.synchronize()
         return prob
 

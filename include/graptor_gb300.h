@@ -249,8 +249,11 @@ GT_API int gt_set_state_device(gt_problem *p, int field, const float *dev);
  * counterpart in the reference, which starts lambda at zero. */
 GT_API int gt_dual_from_primal(gt_problem *p);
 /* gt_dual_from_primal with flags: GT_DUAL_KEEP_EMPTY leaves lambda unchanged on
- * bins without data (f = 0), where the fixed point is mu itself. */
-enum { GT_DUAL_KEEP_EMPTY = 1 };
+ * bins without data (f = 0), where the fixed point is mu itself;
+ * GT_DUAL_CAP10 / GT_DUAL_CAP100: where f > 10 K u (K u = 0 included) set
+ * lambda = mu (1 - cap) with cap 10 / 100 instead of keeping it, a bounded strong
+ * push on rays that the image misses. */
+enum { GT_DUAL_KEEP_EMPTY = 1, GT_DUAL_CAP10 = 2, GT_DUAL_CAP100 = 4 };
 GT_API int gt_dual_from_primal_ex(gt_problem *p, int flags);
 /* The problem's CUDA stream (the one gt_desc.stream named, or its own). */
 GT_API void *gt_problem_stream(gt_problem *p);
