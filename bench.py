@@ -406,7 +406,7 @@ def run_batched(args, rank, world, local):
             "speedup_vs_fixed_shape": out["fixed_shape"]["seconds"] / best["seconds"]}
 
 
-WARM = dict(N=128, Nz=32, C=2, nang=71, pre=500, tol=1e-2, check_every=100, max_iters=40000,
+WARM = dict(N=128, Nz=32, C=2, nang=71, pre=500, tol=1e-2, check_every=100, max_iters=40000, fallback_after=1000,
             weights=os.path.join(ROOT, "graptor_gb300", "weights", "unet_tgv_kl_c2_p500.npz"))
 
 
@@ -414,8 +414,9 @@ def run_warmstart(args, rank, world, local):
     """Time to relative primal-dual gap <= tol on held-out seeded problems
     (3-D TGV-KL, FROB, 2 channels, 128^2 x 32, 71 angles): the plain solver
     cold-started, problems one after another, against the learned warm start
-    (pre cold iterations, U-Net prediction of u, lambda from K u) with all
-    problems advanced together as one Batch.  Set-up (buffers, data upload,
+    (pre cold iterations, U-Net prediction of u, lambda from K u; a problem
+    whose gap is still infinite fallback_after iterations later goes back to
+    its cold iterate) with all problems advanced together as one Batch.  Set-up (buffers, data upload,
     operator norm, autotuning) is outside both timed regions; gap checks every
     check_every iterations are inside both."""
     import math
@@ -456,15 +457,21 @@ def run_warmstart(args, rank, world, local):
         t0 = time.perf_counter()
         b.run(WARM["pre"]).synchronize()
         ws = WS.WarmStarter(net, ("u",), pre_iters=0)
-        for k, (f, _) in enumerate(cases):
-            ws.apply(b[k], f)
+        snaps = [ws.apply(b[k], f, keep_snapshot=True) for k, (f, _) in enumerate(cases)]
         its = WARM["pre"]
+        fell_back = [False] * len(cases)
         while any(w is None for w in warm_its) and its < WARM["max_iters"]:
-            b.run(WARM["check_every"])
+            b.run(WARM["check_every"]).synchronize()  # the members' gap evaluations run on their own streams
             its += WARM["check_every"]
             for k in range(len(cases)):
-                if warm_its[k] is None and done(b[k].gap()["relative"]):
+                if warm_its[k] is not None:
+                    continue
+                g = b[k].gap()["relative"]
+                if done(g):
                     warm_its[k] = its
+                elif not fell_back[k] and not math.isfinite(g) and its - WARM["pre"] >= WARM["fallback_after"]:
+                    ws.restore(b[k], snaps[k])  # back to the cold iterate (the plain solver is the fallback)
+                    fell_back[k] = True
         b.synchronize()
         warm_s = time.perf_counter() - t0
     cold_s = max_over_ranks(cold_s, world)
@@ -479,7 +486,7 @@ def run_warmstart(args, rank, world, local):
                        "pre_iterations": WARM["pre"], "check_every": WARM["check_every"],
                        "weights": os.path.relpath(args.weights or WARM["weights"], ROOT)},
             "cold_seconds": cold_s, "warm_batched_seconds": warm_s, "speedup": cold_s / warm_s,
-            "cold_iterations": cold_its, "warm_iterations": warm_its,
+            "cold_iterations": cold_its, "warm_iterations": warm_its, "fell_back_to_cold": fell_back,
             "gpu_launches": lpi * (sum(cold_its) + len(cases) * its)}
 
 

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <climits>
+#include <type_traits>
 #include <math.h>
 
 #include "gt_common.cuh"
@@ -669,6 +670,34 @@ static inline long long threads_for(long long units, int S) {
   return (VW == 8 || VW == 4) ? units * ((S + VW * 32 - 1) / (VW * 32)) * 32 : units * (S / VW);
 }
 
+// One slice per lane, a warp over 32 consecutive slices, the slice chunk outermost:
+// the warps running at a time all work on the same 32 slices of every pixel or
+// bin, so a projector's working set is one 32-slice chunk of the image or
+// sinogram (e.g. 768^2 x 32 x 4 B = 75 MB, inside L2) instead of all S slices.
+struct SlicesWL {
+  int s0;
+  bool va;
+  __device__ __forceinline__ void load(const float *base, float (&r)[1]) const { r[0] = va ? __ldg(base + s0) : 0.f; }
+  __device__ __forceinline__ void loadw(const float *base, float (&r)[1]) const { r[0] = va ? base[s0] : 0.f; }
+  __device__ __forceinline__ void store(float *base, const float (&r)[1]) const { if (va) base[s0] = r[0]; }
+  __device__ __forceinline__ int slice(int) const { return s0; }
+  __device__ __forceinline__ bool valid(int) const { return va; }
+};
+
+__device__ __forceinline__ bool map_thread_wl(long long units, int S, long long &unit, SlicesWL &sl) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long w = t >> 5;
+  const int nblk = (S + 31) / 32;
+  if (w >= units * nblk) return false;
+  const int blk = (int)(w / units);
+  unit = w - (long long)blk * units;
+  sl.s0 = blk * 32 + (int)(threadIdx.x & 31);
+  sl.va = sl.s0 < S;
+  return true;
+}
+
+static inline long long threads_for_wl(long long units, int S) { return units * ((S + 31) / 32) * 32; }
+
 // ===========================================================================
 // forward projection: kernel `radon` (3-D :773-816).  Ray (i, j) of slice s:
 // acc = sum over rows y and x in [x_low, x_high] of (1 - |x X + y Y + off - i|)+ img.
@@ -790,9 +819,9 @@ __device__ __forceinline__ float mac(float acc, float w, float v) {
   return EXACT ? __fadd_rn(acc, __fmul_rn(w, v)) : __fmaf_rn(w, v, acc);
 }
 
-template <int VW, bool EXACT, int UNR>
+template <int VW, bool EXACT, int UNR, class SL>
 __device__ __forceinline__ void radon_table(const float *__restrict__ img, size_t S, const int2 *__restrict__ ent,
-                                            int n, const Slices<VW> &sl, float (&acc)[VW]) {
+                                            int n, const SL &sl, float (&acc)[VW]) {
 #pragma unroll
   for (int k = 0; k < VW; ++k) acc[k] = 0.f;
   // groups of UNR entries; the next group's entries are fetched while the current
@@ -831,20 +860,27 @@ __device__ __forceinline__ void radon_table(const float *__restrict__ img, size_
 }
 
 // k_fwd: radon of ubar fused with update_lambda_KL (3-D :690-704) or _L2 (:677-688).
-template <int DISC, int VW, int UNR>
+template <int DISC, int VW, int UNR, bool WL = false>
 __global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
   const Dims d = P.d;
   long long unit;
-  Slices<VW> sl;
-  if (!map_thread<VW>((long long)d.nd * d.nang, d.S, unit, sl)) return;
+  typename std::conditional<WL, SlicesWL, Slices<VW>>::type sl;
+  if constexpr (WL) {
+    static_assert(VW == 1, "one slice per lane");
+    if (!map_thread_wl((long long)d.nd * d.nang, d.S, unit, sl)) return;
+  } else {
+    if (!map_thread<VW>((long long)d.nd * d.nang, d.S, unit, sl)) return;
+  }
   const int b = (int)unit;
   const int j = b / d.nd, i = b - j * d.nd;
   float acc[VW];
   if (P.ray_start) {
     const long long r0 = __ldg(P.ray_start + b), r1 = __ldg(P.ray_start + b + 1);
     radon_table<VW, false, UNR>(P.ubar, d.S, P.ray_ent + r0, (int)(r1 - r0), sl, acc);
-  } else {
+  } else if constexpr (!WL) {
     radon_ray<VW>(P.ubar, d.S, d.N, __ldg(P.ofs + j), i, sl, acc);
+  } else {
+    acc[0] = 0.f;  // not reached: the launcher offers the WL shape only with the ray table
   }
   const size_t q = (size_t)b * d.S;
   sl.store(P.ku + q, acc);
@@ -871,10 +907,10 @@ __global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
 // back projection: kernel `radon_ad` (3-D :818-844): linear interpolation
 // between detector bins floor(t) and floor(t)+1 at t = dot((x, y, 1, 0), ofs[j]).
 // ===========================================================================
-template <int VW, bool EXACT = true, int AU = 1>
+template <int VW, bool EXACT = true, int AU = 1, class SL = Slices<VW>>
 __device__ __forceinline__ void radon_ad_pixel(const float *__restrict__ lam, size_t S, int nd, int nang,
                                                const float4 *__restrict__ ofs, float xf, float yf,
-                                               const Slices<VW> &sl, float (&acc)[VW]) {
+                                               const SL &sl, float (&acc)[VW]) {
 #pragma unroll
   for (int k = 0; k < VW; ++k) acc[k] = 0.f;
   const float fnd = (float)nd;
@@ -988,9 +1024,9 @@ __device__ __forceinline__ void bp_tap(float (&acc)[VW], float w, const float (&
   for (int k = 0; k < VW; ++k) acc[k] = mac<EXACT>(acc[k], w, v[k]);
 }
 
-template <int VW, bool EXACT, int AU>
+template <int VW, bool EXACT, int AU, class SL>
 __device__ __forceinline__ void radon_ad_table(const float *__restrict__ lam, size_t S, int nd, int nang,
-                                               const int2 *__restrict__ tab, const Slices<VW> &sl,
+                                               const int2 *__restrict__ tab, const SL &sl,
                                                float (&acc)[VW]) {
 #pragma unroll
   for (int k = 0; k < VW; ++k) acc[k] = 0.f;
@@ -1213,12 +1249,17 @@ __global__ void __launch_bounds__(256) k_bp_run(const IterParams P) {
 
 // k_bp: back projection K* lambda of every (pixel, slice) into P.kstar; it only
 // needs lambda, so it runs beside k_dual.
-template <int VW, int AU, bool TAB>
+template <int VW, int AU, bool TAB, bool WL = false>
 __global__ void __launch_bounds__(256) k_bp(const IterParams P) {
   const Dims d = P.d;
   long long unit;
-  Slices<VW> sl;
-  if (!map_thread<VW>((long long)d.N * d.N, d.S, unit, sl)) return;
+  typename std::conditional<WL, SlicesWL, Slices<VW>>::type sl;
+  if constexpr (WL) {
+    static_assert(VW == 1 && !TAB, "one slice per lane, geometry on the fly");
+    if (!map_thread_wl((long long)d.N * d.N, d.S, unit, sl)) return;
+  } else {
+    if (!map_thread<VW>((long long)d.N * d.N, d.S, unit, sl)) return;
+  }
   const int pix = (int)unit;
   float acc[VW];
   if (TAB && P.bp_tab) {
@@ -1807,13 +1848,15 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // k_bp configs 0..7 = (slices per lane, angles per step, geometry) = (8, 2, table),
 // (8, 4, table), (4, 2, table), (4, 4, table), (8, 1, on the fly), (4, 1, on the fly),
 // (8, 2, on the fly), (4, 2, on the fly); configs 9..12 = (slices per lane,
-// pixels per run) of k_bp_run = (8, 4), (4, 8), (8, 8), (4, 4).
+// pixels per run) of k_bp_run = (8, 4), (4, 8), (8, 8), (4, 4).  k_fwd config 9 and
+// k_bp config 13: one slice per lane with the 32-slice chunk outermost (SlicesWL),
+// for images and sinograms larger than L2.
 // Otherwise one fixed shape with 2 or 1 slices per thread.
 // One more candidate each: one slice per thread (k_fwd config 4, k_bp config 8),
 // which keeps all lanes busy when S is small.
 int num_proj_configs(int S, int which) {
   if (S % 4 != 0) return 1;
-  return which == 0 ? 9 : 13;  // configs 4 / 8 (one slice per thread) stay candidates for every S
+  return which == 0 ? 10 : 14;  // configs 4 / 8 (one slice per thread) stay candidates for every S
 }
 
 template <int VW, int UNR>
@@ -1821,6 +1864,12 @@ static void fwd_vw(const IterParams &P, int disc, cudaStream_t st) {
   const unsigned g = blocks_for(threads_for<VW>((long long)P.d.nd * P.d.nang, P.d.S), 256);
   if (disc == KL) k_fwd<KL, VW, UNR><<<g, 256, 0, st>>>(P);
   else k_fwd<L2, VW, UNR><<<g, 256, 0, st>>>(P);
+}
+
+static void fwd_wl(const IterParams &P, int disc, cudaStream_t st) {
+  const unsigned g = blocks_for(threads_for_wl((long long)P.d.nd * P.d.nang, P.d.S), 256);
+  if (disc == KL) k_fwd<KL, 1, 8, true><<<g, 256, 0, st>>>(P);
+  else k_fwd<L2, 1, 8, true><<<g, 256, 0, st>>>(P);
 }
 
 template <int VW, int R>
@@ -1843,6 +1892,9 @@ cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
       case 6: fwd_run<8, 4>(P, disc, st); break;
       case 7: fwd_run<4, 4>(P, disc, st); break;
       case 8: fwd_run<4, 8>(P, disc, st); break;
+      case 9:
+        if (P.ray_start) fwd_wl(P, disc, st); else fwd_vw<8, 4>(P, disc, st);  // WL streams the ray table
+        break;
       default: fwd_vw<8, 4>(P, disc, st); break;
     }
   } else if (S % 2 == 0) {
@@ -1856,6 +1908,10 @@ cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
 template <int VW, int AU, bool TAB = true>
 static void bp_vw(const IterParams &P, cudaStream_t st) {
   k_bp<VW, AU, TAB><<<blocks_for(threads_for<VW>((long long)P.d.N * P.d.N, P.d.S), 256), 256, 0, st>>>(P);
+}
+
+static void bp_wl(const IterParams &P, cudaStream_t st) {
+  k_bp<1, 1, false, true><<<blocks_for(threads_for_wl((long long)P.d.N * P.d.N, P.d.S), 256), 256, 0, st>>>(P);
 }
 
 template <int VW, int R>
@@ -1880,6 +1936,7 @@ cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
       case 10: bp_run<4, 8>(P, st); break;
       case 11: bp_run<8, 8>(P, st); break;
       case 12: bp_run<4, 4>(P, st); break;
+      case 13: bp_wl(P, st); break;
       default: bp_vw<8, 2>(P, st); break;
     }
   } else if (S % 2 == 0) {

@@ -357,7 +357,31 @@ class WarmStarter:
         torch.cuda.synchronize(net.dev)
         return out[0].cpu().numpy()
 
-    def apply(self, prob, f: np.ndarray):
+    STATE = ("u", "ubar", "p", "pbar", "v", "w", "lambda")
+
+    def snapshot(self, prob) -> dict:
+        """Device copies of the iterate (for the cold-start fallback)."""
+        import torch
+        lib = L.lib()
+        snap = {}
+        for fl in self.STATE:
+            n = int(np.prod(prob._shape(fl)))
+            t = torch.empty(n, dtype=torch.float32, device=self.net.dev)
+            _ck(lib.gt_get_state_device(prob._h, L.FIELDS[fl], _p(t)))
+            snap[fl] = t
+        prob.synchronize()
+        return snap
+
+    def restore(self, prob, snap: dict):
+        lib = L.lib()
+        for fl, t in snap.items():
+            _ck(lib.gt_set_state_device(prob._h, L.FIELDS[fl], _p(t)))
+        prob.synchronize()
+
+    def apply(self, prob, f: np.ndarray, keep_snapshot: bool = False):
+        """Run pre_iters cold iterations, then write the network's prediction
+        into the solver.  With keep_snapshot, returns device copies of the
+        iterate before the prediction (see :func:`solve_warm`)."""
         import torch
         net = self.net
         if prob.dim != 3:
@@ -370,6 +394,7 @@ class WarmStarter:
         st = lib.gt_problem_stream(prob._h)
         if self.pre_iters:
             prob.run(self.pre_iters)
+        snap = self.snapshot(prob) if keep_snapshot else None
         vol = Nz * N * N
         sc = channel_scales(f, C, Nz, N, prob.nang)
         back_np = field_scales(self.fields, sc, prob.alpha, prob.scalars["normest"])
@@ -401,7 +426,7 @@ class WarmStarter:
         if self.reset_dual:
             _ck(lib.gt_dual_from_primal_ex(prob._h, (1 if self.keep_empty else 0) | {0: 0, 10: 2, 100: 4}[self.cap]))
         prob.synchronize()
-        return prob
+        return snap if keep_snapshot else prob
 
 
 # ---------------------------------------------------------------------- data, training, evaluation
@@ -497,6 +522,28 @@ def train(net: UNet3D, xs: np.ndarray, ys: np.ndarray, steps: int = 2000, batch:
     return hist
 
 
+def solve_warm(prob, f, ws: "WarmStarter", tol: float, check_every: int = 100, max_iters: int = 40000,
+               fallback_after: int = 1000):
+    """Warm start, then iterate to relative gap <= tol.  If the gap is still not
+    finite fallback_after iterations after the prediction (K u = 0 on a bin with
+    data: the predicted image misses a ray the data sees), the iterate from
+    before the prediction is restored and the cold iteration continues from it
+    -- the plain solver is the fallback.  Returns (iterations including the cold
+    ones before the prediction, gap, fell_back)."""
+    snap = ws.apply(prob, f, keep_snapshot=True)
+    done, fell_back = ws.pre_iters, False
+    g = prob.gap()["relative"]
+    while not (math.isfinite(g) and g <= tol) and done < max_iters:
+        prob.run(check_every)
+        done += check_every
+        g = prob.gap()["relative"]
+        if not fell_back and not math.isfinite(g) and done - ws.pre_iters >= fallback_after:
+            ws.restore(prob, snap)
+            fell_back = True
+            g = prob.gap()["relative"]
+    return done, g, fell_back
+
+
 def iterations_to_gap(prob, tol: float, check_every: int = 100, max_iters: int = 100000):
     """Iterate until the relative gap is finite and <= tol; returns (iterations, gap).
     (An infinite primal energy -- K u = 0 on a bin with data -- counts as not converged.)"""
@@ -531,15 +578,18 @@ def evaluate(net: UNet3D, seeds, N, Nz, C=2, nang=71, mu=(0.2, 5e-4), alpha=(4.0
                 torch.cuda.synchronize(device)
                 t0 = time.perf_counter()
                 extra = 0
+                fell_back = False
                 if mode == "warm":
-                    ws.apply(p, f)
-                    extra = pre_iters
-                elif mode == "reset":
-                    p.run(pre_iters).dual_from_primal()
-                    extra = pre_iters
-                it, g = iterations_to_gap(p, tol, check_every, max_iters)
+                    it, g, fell_back = solve_warm(p, f, ws, tol, check_every, max_iters)
+                else:
+                    if mode == "reset":
+                        p.run(pre_iters).dual_from_primal()
+                        extra = pre_iters
+                    it, g = iterations_to_gap(p, tol, check_every, max_iters)
                 p.synchronize()
                 row[mode] = {"iterations": it + extra, "gap": g, "seconds": time.perf_counter() - t0}
+                if mode == "warm":
+                    row[mode]["fell_back"] = fell_back
                 finals[mode] = p.get("u")
         for mode in ("reset", "warm"):
             row[mode]["distance_to_cold"] = float(np.linalg.norm(finals[mode] - finals["cold"]) /
