@@ -406,7 +406,7 @@ def run_batched(args, rank, world, local):
             "speedup_vs_fixed_shape": out["fixed_shape"]["seconds"] / best["seconds"]}
 
 
-WARM = dict(N=128, Nz=32, C=2, nang=71, pre=500, tol=1e-2, check_every=100, max_iters=40000, fallback_after=1000,
+WARM = dict(N=128, Nz=32, C=2, nang=71, pre=500, tol=1e-2, check_every=100, max_iters=40000, fallback_after=10000,
             weights=os.path.join(ROOT, "graptor_gb300", "weights", "unet_tgv_kl_c2_p500.npz"))
 
 
@@ -469,6 +469,7 @@ def run_warmstart(args, rank, world, local):
                 g = b[k].gap()["relative"]
                 if done(g):
                     warm_its[k] = its
+                    b.set_active(k, False)  # converged: the batch goes on without it
                 elif not fell_back[k] and not math.isfinite(g) and its - WARM["pre"] >= WARM["fallback_after"]:
                     ws.restore(b[k], snaps[k])  # back to the cold iterate (the plain solver is the fallback)
                     fell_back[k] = True

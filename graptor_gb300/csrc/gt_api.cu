@@ -803,6 +803,7 @@ struct gt_batch {
   int chunk = 8;
   int chains = 8;  // problems are spread over this many concurrent chains
   long long iters = 0;
+  std::vector<char> active;  // problems advanced by gt_batch_run
 };
 
 // One iteration of every problem: problem k runs on chain k % chains; chains run
@@ -812,19 +813,22 @@ static int batch_capture(gt_batch *b, int n, cudaGraphExec_t *out) {
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   int rc = GT_OK;
   cudaError_t e = cudaSuccess;
-  const size_t np = b->probs.size();
+  std::vector<size_t> act;  // the active problems, in order
+  for (size_t k = 0; k < b->probs.size(); ++k)
+    if (b->active[k]) act.push_back(k);
+  const size_t np = act.size();
   const size_t chains = std::max<size_t>(1, std::min<size_t>(np, (size_t)b->chains));
   for (int it = 0; it < n && rc == GT_OK && e == cudaSuccess; ++it) {
     e = cudaEventRecord(b->fork, b->stream);
     for (size_t k = 0; k < np && rc == GT_OK && e == cudaSuccess; ++k) {
-      gt_problem *p = b->probs[k];
+      gt_problem *p = b->probs[act[k]];
       // first problem of a chain waits for the fork, the others for their predecessor
-      e = cudaStreamWaitEvent(p->stream, k < chains ? b->fork : b->joins[k - chains], 0);
+      e = cudaStreamWaitEvent(p->stream, k < chains ? b->fork : b->joins[act[k - chains]], 0);
       if (e == cudaSuccess) rc = enqueue_iteration(p);
-      if (rc == GT_OK && e == cudaSuccess) e = cudaEventRecord(b->joins[k], p->stream);
+      if (rc == GT_OK && e == cudaSuccess) e = cudaEventRecord(b->joins[act[k]], p->stream);
     }
     for (size_t k = np - std::min(np, chains); k < np && rc == GT_OK && e == cudaSuccess; ++k)
-      e = cudaStreamWaitEvent(b->stream, b->joins[k], 0);
+      e = cudaStreamWaitEvent(b->stream, b->joins[act[k]], 0);
   }
   cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
   if (rc != GT_OK || e != cudaSuccess || e2 != cudaSuccess) {
@@ -878,8 +882,21 @@ int gt_batch_create(int n, const gt_desc *descs, gt_batch **out) {
       return cuda_err(e, "batch events", __LINE__);
     }
     b->joins.push_back(ev);
+    b->active.push_back(1);
   }
   *out = b;
+  return GT_OK;
+}
+
+int gt_batch_set_active(gt_batch *b, int k, int active) {
+  if (!b || k < 0 || k >= (int)b->probs.size()) return set_err(GT_ERR_ARG, "gt_batch_set_active: bad index");
+  if ((b->active[k] != 0) == (active != 0)) return GT_OK;
+  CK(cudaSetDevice(b->device));
+  CK(cudaStreamSynchronize(b->stream));
+  b->active[k] = active ? 1 : 0;
+  // the captured graphs hold the old member set
+  if (b->g_chunk) { cudaGraphExecDestroy(b->g_chunk); b->g_chunk = nullptr; }
+  if (b->g_one) { cudaGraphExecDestroy(b->g_one); b->g_one = nullptr; }
   return GT_OK;
 }
 
@@ -897,6 +914,7 @@ int gt_batch_run(gt_batch *b, int iters) {
   for (auto p : b->probs)
     if (!p->has_data) return set_err(GT_ERR_STATE, "gt_batch_run before every problem has data");
   if (iters == 0) return GT_OK;
+  if (std::find(b->active.begin(), b->active.end(), 1) == b->active.end()) return GT_OK;  // nothing active
   CK(cudaSetDevice(b->device));
   // problems' own streams may still carry set-up work: the batch stream waits for it
   for (size_t k = 0; k < b->probs.size(); ++k) {
@@ -909,7 +927,8 @@ int gt_batch_run(gt_batch *b, int iters) {
   int left = iters;
   while (left >= b->chunk) { CK(cudaGraphLaunch(b->g_chunk, b->stream)); left -= b->chunk; }
   while (left > 0) { CK(cudaGraphLaunch(b->g_one, b->stream)); --left; }
-  for (auto p : b->probs) p->iters += iters;
+  for (size_t k = 0; k < b->probs.size(); ++k)
+    if (b->active[k]) b->probs[k]->iters += iters;
   b->iters += iters;
   return GT_OK;
 }

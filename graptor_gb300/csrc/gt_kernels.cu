@@ -1376,14 +1376,20 @@ __global__ void k_fill(T *__restrict__ x, size_t n, T v) {
 // ===========================================================================
 // FP64 operator-norm power iteration (radon_normest, 3-D :1018-1030), one slice
 // ===========================================================================
-__global__ void k_radon64(const double *__restrict__ img, double *__restrict__ sino, const dvec4 *__restrict__ ofs,
-                          int N, int nd, int nang) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nd * nang) return;
-  const int j = t / nd, i = t - j * nd;
+// FP64 forward projection of one slice, a warp per ray: lane l sums rows l, l+32,
+// ..., then a fixed butterfly adds the 32 partial sums (deterministic).  Weights
+// and bounds as the float projector, in double (the x range is widened by one
+// pixel and the weight test decides).
+__global__ void k_radon64_warp(const double *__restrict__ img, double *__restrict__ sino,
+                               const dvec4 *__restrict__ ofs, int N, int nd, int nang) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long ray = t >> 5;
+  const int lane = threadIdx.x & 31;
+  if (ray >= (long long)nd * nang) return;  // whole warps leave together
+  const int j = (int)(ray / nd), i = (int)(ray - (long long)j * nd);
   const dvec4 o = ofs[j];
   double acc = 0.0;
-  for (int y = 0; y < N; ++y) {
+  for (int y = lane; y < N; y += 32) {
     const double dd = y * o.y + o.z;
     int xl, xh;
     if (o.x == 0.0) {
@@ -1399,7 +1405,9 @@ __global__ void k_radon64(const double *__restrict__ img, double *__restrict__ s
       if (wgt > 0.0) acc += wgt * img[(size_t)y * N + x];
     }
   }
-  sino[t] = acc;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if (lane == 0) sino[ray] = acc;
 }
 
 __global__ void k_radon_ad64(const double *__restrict__ sino, double *__restrict__ img, const dvec4 *__restrict__ ofs,
@@ -2085,7 +2093,7 @@ cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, dou
     k_sum64_partial<<<nb, 256, 0, st>>>(d_img, n, d_part);
     k_sum64_partial<<<1, 256, 0, st>>>(d_part, nb, d_part + nb);
     k_scale64<<<64, 256, 0, st>>>(d_img, n, d_part + nb);
-    k_radon64<<<blocks_for((long long)nd * nang, 128), 128, 0, st>>>(d_img, d_sino, ofs, N, nd, nang);
+    k_radon64_warp<<<blocks_for(32LL * nd * nang, 256), 256, 0, st>>>(d_img, d_sino, ofs, N, nd, nang);
     k_radon_ad64<<<blocks_for((long long)n, 128), 128, 0, st>>>(d_sino, d_img, ofs, N, nd, nang);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }

@@ -231,6 +231,11 @@ class Batch:
     def invalidate(self):
         L.check(L.lib().gt_batch_invalidate(self._b))
 
+    def set_active(self, k: int, active: bool = True):
+        """Leave problem k out of (or bring it back into) the following runs."""
+        L.check(L.lib().gt_batch_set_active(self._b, int(k), int(bool(active))))
+        return self
+
     def set_concurrency(self, chains: int):
         """Spread the problems over `chains` concurrent chains (default 8)."""
         L.check(L.lib().gt_batch_set_concurrency(self._b, int(chains)))

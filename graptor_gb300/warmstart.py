@@ -523,7 +523,7 @@ def train(net: UNet3D, xs: np.ndarray, ys: np.ndarray, steps: int = 2000, batch:
 
 
 def solve_warm(prob, f, ws: "WarmStarter", tol: float, check_every: int = 100, max_iters: int = 40000,
-               fallback_after: int = 1000):
+               fallback_after: int = 10000):
     """Warm start, then iterate to relative gap <= tol.  If the gap is still not
     finite fallback_after iterations after the prediction (K u = 0 on a bin with
     data: the predicted image misses a ray the data sees), the iterate from

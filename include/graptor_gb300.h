@@ -179,6 +179,10 @@ GT_API int gt_batch_invalidate(gt_batch *b);
 /* Run the batch's problems on `chains` concurrent chains (problem k on chain
  * k mod chains, one after another within a chain); default 8. */
 GT_API int gt_batch_set_concurrency(gt_batch *b, int chains);
+/* Leave problem k out of (active = 0) or bring it back into (1) the following
+ * gt_batch_run calls, e.g. once it has reached its gap tolerance; its state is
+ * kept.  All problems are active after gt_batch_create. */
+GT_API int gt_batch_set_active(gt_batch *b, int k, int active);
 
 /* Kernels of the learned warm start (a small 3-D U-Net whose output initialises
  * the solver's image).  No counterpart in the reference, which always starts

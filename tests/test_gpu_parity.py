@@ -338,6 +338,25 @@ def test_batch_matches_individual_problems():
         with Problem(**sp) as p:
             p.set_data(datas[k]).run(37).synchronize()
             np.testing.assert_array_equal(got[k], p.get("u"), err_msg=f"member {k}")
+    # members left out of some runs keep their state and resume exactly
+    with Batch(specs) as b:
+        for k in range(len(b)):
+            b[k].set_data(datas[k])
+        b.run(20)
+        b.set_active(1, False).set_active(3, False)
+        b.run(17).synchronize()
+        held = [b[k].get("u") for k in (1, 3)]
+        b.set_active(1, True).set_active(3, True)
+        b.run(17).synchronize()
+        out = [b[k].get("u") for k in range(len(b))]
+    its = {0: 54, 1: 37, 2: 54, 3: 37}
+    for k, sp in enumerate(specs):
+        with Problem(**sp) as p:
+            p.set_data(datas[k]).run(its[k]).synchronize()
+            np.testing.assert_array_equal(out[k], p.get("u"), err_msg=f"member {k} after pause")
+            if k in (1, 3):
+                p.set_data(datas[k]).run(20).synchronize()
+                np.testing.assert_array_equal(held[(k - 1) // 2], p.get("u"), err_msg=f"member {k} paused")
 
 
 def test_out_of_memory_is_a_memory_error():
