@@ -80,7 +80,7 @@ _SIGS = {
     "gt_set_state_device": (ctypes.c_int, [_P, ctypes.c_int, _P]),
     "gt_problem_stream": (ctypes.c_void_p, [_P]),
     "gt_dual_from_primal": (ctypes.c_int, [_P]),
-    "gt_dual_from_primal_ex": (ctypes.c_int, [_P, _I]),
+    "gt_dual_from_primal_ex": (ctypes.c_int, [_P, _I, ctypes.c_float]),
     "gt_set_tuning": (ctypes.c_int, [_P, _I, _I]),
     "gt_set_dual_shape": (ctypes.c_int, [_P, _I]),
     "gt_get_dual_shape": (ctypes.c_int, [_P]),

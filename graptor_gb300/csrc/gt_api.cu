@@ -31,7 +31,9 @@ cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, in
 cudaError_t launch_transpose(const float *in, float *out, int rows, int cols, cudaStream_t st);
 cudaError_t launch_feasible(float *f, const float *r1, int nbin1, int S, cudaStream_t st);
 cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
-                                int Nz, int disc, int keep_empty, float cap, cudaStream_t st);
+                                int Nz, int disc, float empty_weight, float cap, cudaStream_t st);
+cudaError_t launch_missed_rays(const float *ku, const float *f, float *r, long long n, int N, cudaStream_t st);
+cudaError_t launch_add2(float *a, float *b, const float *d, long long n, cudaStream_t st);
 cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, double *d_img, double *d_sino,
                       double *d_part, double *out, cudaStream_t st);
 cudaError_t fill_f64(double *x, size_t n, double v, cudaStream_t st);
@@ -613,20 +615,31 @@ int gt_set_state_device(gt_problem *p, int field, const float *dev) {
   return GT_OK;
 }
 
-int gt_dual_from_primal_ex(gt_problem *p, int flags) {
+int gt_dual_from_primal_ex(gt_problem *p, int flags, float empty_weight) {
   if (!p) return set_err(GT_ERR_ARG, "null argument");
   if (!p->has_data) return set_err(GT_ERR_STATE, "gt_dual_from_primal before gt_set_data");
-  if (flags & ~(GT_DUAL_KEEP_EMPTY | GT_DUAL_CAP10 | GT_DUAL_CAP100)) return set_err(GT_ERR_ARG, "unknown flags %d", flags);
+  if (flags & ~(GT_DUAL_CAP10 | GT_DUAL_CAP100 | GT_DUAL_REPAIR | GT_DUAL_NO_RESET))
+    return set_err(GT_ERR_ARG, "unknown flags %d", flags);
+  if (!(empty_weight >= 0.f && empty_weight <= 1.f)) return set_err(GT_ERR_ARG, "empty_weight must lie in [0, 1]");
   const float cap = (flags & GT_DUAL_CAP100) ? 100.f : ((flags & GT_DUAL_CAP10) ? 10.f : 0.f);
   CK(cudaSetDevice(p->device));
   // K u into the ku buffer (the next iteration's forward projection overwrites it)
   CK(gt::launch_radon(p->u, p->ku, p->ofs, p->d.N, p->d.nd, p->d.nang, p->d.S, p->stream));
+  if ((flags & GT_DUAL_REPAIR) && p->disc == GT_KL) {
+    // lift u along rays with data that the image misses: u, ubar += R^T r (stage holds
+    // the image-sized correction), then project again
+    CK(gt::launch_missed_rays(p->ku, p->f, p->ku, (long long)p->d.nbin, p->d.N, p->stream));
+    CK(gt::launch_radon_ad(p->ku, p->stage, p->ofs, p->d.N, p->d.nd, p->d.nang, p->d.S, p->stream));
+    CK(gt::launch_add2(p->u, p->ubar, p->stage, (long long)p->d.vol, p->stream));
+    CK(gt::launch_radon(p->u, p->ku, p->ofs, p->d.N, p->d.nd, p->d.nang, p->d.S, p->stream));
+  }
+  if (flags & GT_DUAL_NO_RESET) return GT_OK;  // only the lift
   CK(gt::launch_lambda_fixed(p->lam, p->ku, p->f, p->mu64, (long long)p->d.nd * p->d.nang, p->d.S, p->d.Nz, p->disc,
-                             (flags & GT_DUAL_KEEP_EMPTY) ? 1 : 0, cap, p->stream));
+                             empty_weight, cap, p->stream));
   return GT_OK;
 }
 
-int gt_dual_from_primal(gt_problem *p) { return gt_dual_from_primal_ex(p, 0); }
+int gt_dual_from_primal(gt_problem *p) { return gt_dual_from_primal_ex(p, 0, 1.f); }
 
 void *gt_problem_stream(gt_problem *p) { return p ? (void *)p->stream : nullptr; }
 

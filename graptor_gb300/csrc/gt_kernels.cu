@@ -1346,13 +1346,17 @@ __global__ void k_feasible(float *__restrict__ f, const float *__restrict__ r1, 
 // below and would throw the next primal step far off, so lambda is kept.
 // L2 (update_lambda_L2, :677-688, weight m = mu / (sigma + mu)): lam = mu (ku - f).
 __global__ void k_lambda_fixed(float *__restrict__ lam, const float *__restrict__ ku, const float *__restrict__ f,
-                               const double *__restrict__ mu, long long nbin, int S, int Nz, int disc, int keep_empty,
-                               float cap) {
+                               const double *__restrict__ mu, long long nbin, int S, int Nz, int disc,
+                               float empty_weight, float cap) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nbin * S) return;
   const int s = (int)(t % S);
   const float m = (float)mu[s / Nz], k = ku[t], fv = f[t];
-  if (keep_empty && fv == 0.f) return;
+  if (fv == 0.f && empty_weight < 1.f) {  // bins without data move only part of the way to mu
+    if (disc == 0 && k > 0.f) lam[t] = lam[t] + empty_weight * (m - lam[t]);
+    if (disc != 0) lam[t] = lam[t] + empty_weight * (m * k - lam[t]);
+    return;
+  }
   if (disc == 0) {
     if (k > 0.f && fv <= 10.f * k) lam[t] = m * (1.0f - fv / k);
     else if (cap > 0.f && fv > 0.f) lam[t] = m * (1.0f - cap);  // f / K u capped: a strong push up the ray
@@ -1361,9 +1365,36 @@ __global__ void k_lambda_fixed(float *__restrict__ lam, const float *__restrict_
   }
 }
 
+// Rays the image misses: r = f / N where the data has counts (f > 0) but K u = 0,
+// else 0.  Back-projected and added to u, it makes K u > 0 on those bins (about
+// f / 2 there) so that the KL data term, and with it the primal value, is finite.
+__global__ void k_missed_rays(const float *__restrict__ ku, const float *__restrict__ f, float *__restrict__ r,
+                              long long n, float inv_n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  r[t] = (f[t] > 0.f && !(ku[t] > 0.f)) ? f[t] * inv_n : 0.f;
+}
+
+__global__ void k_add2(float *__restrict__ a, float *__restrict__ b, const float *__restrict__ d, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  a[t] += d[t];
+  b[t] += d[t];
+}
+
+cudaError_t launch_missed_rays(const float *ku, const float *f, float *r, long long n, int N, cudaStream_t st) {
+  k_missed_rays<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ku, f, r, n, 1.f / (float)N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add2(float *a, float *b, const float *d, long long n, cudaStream_t st) {
+  k_add2<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, b, d, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
-                                int Nz, int disc, int keep_empty, float cap, cudaStream_t st) {
-  k_lambda_fixed<<<(unsigned)((nbin * S + 255) / 256), 256, 0, st>>>(lam, ku, f, mu, nbin, S, Nz, disc, keep_empty,
+                                int Nz, int disc, float empty_weight, float cap, cudaStream_t st) {
+  k_lambda_fixed<<<(unsigned)((nbin * S + 255) / 256), 256, 0, st>>>(lam, ku, f, mu, nbin, S, Nz, disc, empty_weight,
                                                                       cap);
   return cudaGetLastError();
 }

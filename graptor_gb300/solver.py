@@ -142,12 +142,19 @@ class Problem:
         L.check(L.lib().gt_set_dual_shape(self._h, int(cfg)))
         return self
 
-    def dual_from_primal(self, keep_empty: bool = False, cap: int = 0):
-        """Set lambda consistent with the current u (for warm starts); with
-        keep_empty, bins without data keep their lambda; cap 10 or 100 sets
-        lambda = mu (1 - cap) where f > 10 K u (see gt_dual_from_primal_ex)."""
-        flags = (1 if keep_empty else 0) | {0: 0, 10: 2, 100: 4}[int(cap)]
-        L.check(L.lib().gt_dual_from_primal_ex(self._h, flags))
+    def dual_from_primal(self, empty_weight: float = 1.0, cap: int = 0, repair: bool = False):
+        """Set lambda consistent with the current u (for warm starts); bins
+        without data move empty_weight of the way to their fixed point; cap 10
+        or 100 sets lambda = mu (1 - cap) where f > 10 K u; repair first lifts u
+        along rays with data that it misses (gt_dual_from_primal_ex)."""
+        flags = {0: 0, 10: 2, 100: 4}[int(cap)] | (8 if repair else 0)
+        L.check(L.lib().gt_dual_from_primal_ex(self._h, flags, float(empty_weight)))
+        return self
+
+    def repair_missed_rays(self):
+        """Lift u (and ubar) along rays with data that the image misses (K u = 0
+        < f, KL), leaving lambda: the primal value becomes finite again."""
+        L.check(L.lib().gt_dual_from_primal_ex(self._h, 8 | 16, 1.0))
         return self
 
     @property

@@ -336,11 +336,12 @@ class WarmStarter:
     that the first iterations pull u back towards the cold-start state."""
 
     def __init__(self, net: UNet3D, fields=("u", "v"), pre_iters: int = 20, use=None, reset_dual: bool = True,
-                 keep_empty: bool = False, cap: int = 0):
+                 empty_weight: float = 1.0, cap: int = 0, repair: bool = True):
         self.net, self.fields, self.pre_iters = net, tuple(fields), int(pre_iters)
         self.use = tuple(use) if use is not None else self.fields  # predicted fields written to the solver
         self.reset_dual = bool(reset_dual)
-        self.keep_empty = bool(keep_empty)  # leave lambda on bins without data
+        self.empty_weight = float(empty_weight)  # fraction of the reset applied on bins without data
+        self.repair = bool(repair)  # lift u along rays with data that the prediction misses
         self.cap = int(cap)  # 0: keep lambda where f > 10 K u; 10 / 100: lambda = mu (1 - cap) there
         if self.fields[0] != "u":
             raise ValueError("the first predicted field must be u (the residual channels)")
@@ -424,7 +425,8 @@ class WarmStarter:
             ch += n
         # the data dual consistent with the predicted image (fixed point of its update)
         if self.reset_dual:
-            _ck(lib.gt_dual_from_primal_ex(prob._h, (1 if self.keep_empty else 0) | {0: 0, 10: 2, 100: 4}[self.cap]))
+            _ck(lib.gt_dual_from_primal_ex(prob._h, {0: 0, 10: 2, 100: 4}[self.cap] | (8 if self.repair else 0),
+                                           self.empty_weight))
         prob.synchronize()
         return snap if keep_snapshot else prob
 
@@ -524,11 +526,12 @@ def train(net: UNet3D, xs: np.ndarray, ys: np.ndarray, steps: int = 2000, batch:
 
 def solve_warm(prob, f, ws: "WarmStarter", tol: float, check_every: int = 100, max_iters: int = 40000,
                fallback_after: int = 10000):
-    """Warm start, then iterate to relative gap <= tol.  If the gap is still not
-    finite fallback_after iterations after the prediction (K u = 0 on a bin with
-    data: the predicted image misses a ray the data sees), the iterate from
-    before the prediction is restored and the cold iteration continues from it
-    -- the plain solver is the fallback.  Returns (iterations including the cold
+    """Warm start, then iterate to relative gap <= tol.  When a check finds the
+    gap not finite (K u = 0 on a bin with data: the image misses a ray the data
+    sees), u is lifted along those rays (:meth:`Problem.repair_missed_rays`); if
+    it is still not finite fallback_after iterations after the prediction, the
+    iterate from before the prediction is restored and the cold iteration
+    continues from it -- the plain solver is the fallback.  Returns (iterations including the cold
     ones before the prediction, gap, fell_back)."""
     snap = ws.apply(prob, f, keep_snapshot=True)
     done, fell_back = ws.pre_iters, False
@@ -537,6 +540,10 @@ def solve_warm(prob, f, ws: "WarmStarter", tol: float, check_every: int = 100, m
         prob.run(check_every)
         done += check_every
         g = prob.gap()["relative"]
+        if not math.isfinite(g) and prob.discrepancy == "KL":
+            # the iterate misses a ray with data (infinite KL value): lift u along it
+            prob.repair_missed_rays()
+            g = prob.gap()["relative"]
         if not fell_back and not math.isfinite(g) and done - ws.pre_iters >= fallback_after:
             ws.restore(prob, snap)
             fell_back = True

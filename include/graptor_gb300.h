@@ -252,13 +252,17 @@ GT_API int gt_set_state_device(gt_problem *p, int field, const float *dev);
  * where f > 10 K u, K u = 0 included; L2: mu (K u - f)).  For warm starts (set u, then this).  No
  * counterpart in the reference, which starts lambda at zero. */
 GT_API int gt_dual_from_primal(gt_problem *p);
-/* gt_dual_from_primal with flags: GT_DUAL_KEEP_EMPTY leaves lambda unchanged on
- * bins without data (f = 0), where the fixed point is mu itself;
+/* gt_dual_from_primal with options.  empty_weight in [0, 1]: on bins without data
+ * (f = 0) lambda moves that fraction of the way to its fixed point (KL: mu,
+ * where K u > 0; L2: mu K u); 1 is gt_dual_from_primal, 0 leaves those bins.
  * GT_DUAL_CAP10 / GT_DUAL_CAP100: where f > 10 K u (K u = 0 included) set
  * lambda = mu (1 - cap) with cap 10 / 100 instead of keeping it, a bounded strong
- * push on rays that the image misses. */
-enum { GT_DUAL_KEEP_EMPTY = 1, GT_DUAL_CAP10 = 2, GT_DUAL_CAP100 = 4 };
-GT_API int gt_dual_from_primal_ex(gt_problem *p, int flags);
+ * push on rays that the image misses.  GT_DUAL_REPAIR (KL): first lift u and ubar
+ * along every ray with data (f > 0) that the image misses (K u = 0) by a back
+ * projection of f / N on those bins, so that the primal value is finite;
+ * GT_DUAL_REPAIR | GT_DUAL_NO_RESET does only that lift and leaves lambda. */
+enum { GT_DUAL_CAP10 = 2, GT_DUAL_CAP100 = 4, GT_DUAL_REPAIR = 8, GT_DUAL_NO_RESET = 16 };
+GT_API int gt_dual_from_primal_ex(gt_problem *p, int flags, float empty_weight);
 /* The problem's CUDA stream (the one gt_desc.stream named, or its own). */
 GT_API void *gt_problem_stream(gt_problem *p);
 

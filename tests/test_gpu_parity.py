@@ -296,6 +296,30 @@ def test_dual_from_primal_is_a_fixed_point(disc):
         assert np.abs(u).sum() > 0
 
 
+def test_dual_reset_repairs_missed_rays():
+    """With repair, an image that misses rays carrying data (K u = 0 < f) is
+    lifted along them first: afterwards K u > 0 wherever f > 0, so the KL primal
+    value (and the gap) is finite, and lambda is finite."""
+    from graptor_gb300 import phantom
+    from graptor_gb300.solver import Problem
+    rng = np.random.default_rng(77)
+    N, Nz, C, nang = 24, 4, 2, 13
+    ang = phantom.angles_deg(nang)
+    f = np.zeros((C * Nz, nang, N), np.float32)
+    f[:, :, 8:14] = np.abs(rng.standard_normal((C * Nz, nang, 6))).astype(np.float32) + 0.1
+    with Problem(3, N, Nz, C, N, ang, (4, 1), [0.2, 0.05], normest=17.0) as p:
+        p.set_data(f, feasible=False)
+        zero = np.zeros((C * Nz, N, N), np.float32)
+        p.set("u", zero)
+        p.set("ubar", zero)
+        p.dual_from_primal(repair=True).synchronize()
+        ku, fd, u, lam = p.get("ku"), p.get("data"), p.get("u"), p.get("lambda")
+        assert (ku[fd > 0] > 0).all()
+        assert np.isfinite(lam).all() and (u >= 0).all() and u.max() > 0
+        assert np.array_equal(p.get("ubar"), u)
+        assert np.isfinite(p.gap()["primal"])
+
+
 def test_fp64_normest_matches_reference_estimate(golden):
     """The FP64 power iteration agrees with the reference's FP32 estimate."""
     from graptor_gb300.solver import Problem
