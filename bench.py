@@ -414,9 +414,11 @@ def run_warmstart(args, rank, world, local):
     """Time to relative primal-dual gap <= tol on held-out seeded problems
     (3-D TGV-KL, FROB, 2 channels, 128^2 x 32, 71 angles): the plain solver
     cold-started, problems one after another, against the learned warm start
-    (pre cold iterations, U-Net prediction of u, lambda from K u; a problem
-    whose gap is still infinite fallback_after iterations later goes back to
-    its cold iterate) with all problems advanced together as one Batch.  Set-up (buffers, data upload,
+    (pre cold iterations, U-Net prediction of u, lambda from K u; at a check
+    that finds a problem's gap infinite, u is lifted along the rays with data
+    it misses; a problem whose gap is still infinite fallback_after iterations
+    after the prediction goes back to its cold iterate) with all problems
+    advanced together as one Batch; converged problems leave the batch.  Set-up (buffers, data upload,
     operator norm, autotuning) is outside both timed regions; gap checks every
     check_every iterations are inside both."""
     import math
@@ -467,6 +469,9 @@ def run_warmstart(args, rank, world, local):
                 if warm_its[k] is not None:
                     continue
                 g = b[k].gap()["relative"]
+                if not math.isfinite(g):
+                    b[k].repair_missed_rays()  # the iterate misses a ray with data: lift u along it
+                    g = b[k].gap()["relative"]
                 if done(g):
                     warm_its[k] = its
                     b.set_active(k, False)  # converged: the batch goes on without it
