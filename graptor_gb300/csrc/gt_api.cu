@@ -42,6 +42,9 @@ cudaError_t launch_ray_count(const float4 *ofs, int N, int nd, int nang, int *co
 cudaError_t launch_ray_fill(const float4 *ofs, int N, int nd, int nang, const long long *start, int2 *ent,
                             cudaStream_t st);
 cudaError_t launch_bp_table(const float4 *ofs, int N, int nd, int nang, int2 *tab, cudaStream_t st);
+cudaError_t launch_run_count(const float4 *ofs, int N, int nd, int nang, int *count, cudaStream_t st);
+cudaError_t launch_run_fill(const float4 *ofs, int N, int nd, int nang, const long long *start, int4 *ent,
+                            cudaStream_t st);
 int num_proj_configs(int S, int which);
 bool dual_z2_ok(const IterParams &P, int tgv, int cpl);
 int gap_blocks(const IterParams &P);
@@ -121,6 +124,7 @@ struct gt_problem {
   float *u = nullptr, *ubar = nullptr, *p = nullptr, *pbar = nullptr, *v = nullptr, *w = nullptr;
   float *lam = nullptr, *f = nullptr, *ku = nullptr, *stage = nullptr, *kstar = nullptr;
   void *rays = nullptr;        // ray table (offsets + entries), built at creation
+  void *runs = nullptr;        // 3-bin run table (offsets + entries), built at creation
   size_t ray_bytes = 0;
   void *gap_ws = nullptr;      // gap workspace (v~ planes + FP64 block partials), allocated on first gt_gap
   double *mu64 = nullptr;
@@ -442,6 +446,36 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
     p->P.bp_tab = (const int2 *)((char *)p->rays + off_bp);
   }
 
+  // 3-bin run table of the forward projector (k_fwd_rt); optional: without it
+  // (no memory) the run shapes fall back to the ray table
+  {
+    const int nr = ((D.nd + 2) / 3) * D.nang;
+    std::vector<int> cnt(nr);
+    std::vector<long long> start(nr + 1, 0);
+    int *d_cnt = (int *)p->stage;
+    if ((e = gt::launch_run_count(p->ofs, D.N, D.nd, D.nang, d_cnt, p->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * nr, cudaMemcpyDeviceToHost, p->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(p->stream)) != cudaSuccess)
+      return fail(cuda_err(e, "run table count", __LINE__));
+    for (int r = 0; r < nr; ++r) start[r + 1] = start[r] + cnt[r];
+    const size_t off_e = align256(sizeof(long long) * (nr + 1));
+    const size_t bytes = off_e + sizeof(int4) * (size_t)start[nr];
+    if (cudaMalloc(&p->runs, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      p->runs = nullptr;
+    } else {
+      long long *d_start = (long long *)p->runs;
+      int4 *d_ent = (int4 *)((char *)p->runs + off_e);
+      if ((e = cudaMemcpyAsync(d_start, start.data(), sizeof(long long) * (nr + 1), cudaMemcpyHostToDevice,
+                               p->stream)) != cudaSuccess ||
+          (e = gt::launch_run_fill(p->ofs, D.N, D.nd, D.nang, d_start, d_ent, p->stream)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(p->stream)) != cudaSuccess)
+        return fail(cuda_err(e, "run table fill", __LINE__));
+      p->P.run_start = d_start;
+      p->P.run_ent = d_ent;
+    }
+  }
+
   gt::IterParams &P = p->P;
   P.d = p->d;
   P.ofs = p->ofs; P.mu = p->mu_eff;
@@ -459,6 +493,7 @@ void gt_problem_destroy(gt_problem *p) {
   if (p->g_chunk) cudaGraphExecDestroy(p->g_chunk);
   if (p->block) cudaFree(p->block);
   if (p->rays) cudaFree(p->rays);
+  if (p->runs) cudaFree(p->runs);
   if (p->gap_ws) cudaFree(p->gap_ws);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);

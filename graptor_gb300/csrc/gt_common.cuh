@@ -46,6 +46,8 @@ struct IterParams {
   const float4 *ofs;     // [nang] (X, Y, offset, Xinv)
   const long long *ray_start;  // [nd*nang + 1] ray table offsets (null: walk rays on the fly)
   const int2 *ray_ent;         // (pixel, weight bits) entries of all rays
+  const long long *run_start;  // [nang*ceil(nd/3) + 1] offsets of the 3-bin run table (null: none)
+  const int4 *run_ent;         // (pixel, weight bits of bins i0, i0+1, i0+2) entries of all runs
   const int2 *bp_tab;          // [N*N][nang] (floor bin, fraction bits) of the back projection (or null)
   const float *mu;       // [C] mu (KL) or mu/(sigma+mu) (L2)
   float *u, *ubar;       // [vol]

@@ -812,6 +812,81 @@ __global__ void k_ray_fill(const float4 *__restrict__ ofs, int N, int nd, int na
   ray_walk<true>(__ldg(ofs + j), i, N, ent + start[t]);
 }
 
+// Run table: the rays of three adjacent bins i0, i0+1, i0+2 of one angle walked
+// together.  Per row the union of their x ranges is listed once, each pixel with
+// its three weights (zero where the bin's hat does not cover it), in the rows-
+// then-x order of the reference; a pixel is loaded once for the three bins.
+// Every weight is the one ray_walk computes for that bin, and a zero weight adds
+// an exact zero, so each bin's sum is the ray table's, term for term.
+template <bool FILL>
+__device__ __forceinline__ int run_walk(const float4 o, int i0, int N, int nd, int4 *out) {
+  int ylo, yhi, ylo2, yhi2;
+  ray_rows(o, i0, N, ylo, yhi);
+  ray_rows(o, min(i0 + 2, nd - 1), N, ylo2, yhi2);
+  ylo = min(ylo, ylo2);
+  yhi = max(yhi, yhi2);
+  int n = 0;
+  for (int y = ylo; y <= yhi; ++y) {
+    const float d = __fadd_rn(__fmul_rn((float)y, o.y), o.z);
+    int xl[3], xh[3];
+    int xmin = N, xmax = -1;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const int i = i0 + r;
+      const float fim = (float)(i - 1), fip = (float)(i + 1);
+      int a, b;
+      if (o.x == 0.f) {
+        if (d > fim && d < fip) { a = 0; b = N - 1; } else { a = N; b = -1; }
+      } else if (o.x > 0.f) {
+        a = __float2int_rz(__fmul_rn(__fsub_rn(fim, d), o.w));
+        b = __float2int_rz(__fmul_rn(__fsub_rn(fip, d), o.w));
+      } else {
+        a = __float2int_rz(__fmul_rn(__fsub_rn(fip, d), o.w));
+        b = __float2int_rz(__fmul_rn(__fsub_rn(fim, d), o.w));
+      }
+      a = max(a, 0);
+      b = min(b, N - 1);
+      if (i >= nd) { a = N; b = -1; }
+      xl[r] = a;
+      xh[r] = b;
+      if (a <= b) { xmin = min(xmin, a); xmax = max(xmax, b); }
+    }
+    for (int x = xmin; x <= xmax; ++x) {
+      const float tx = __fadd_rn(__fmul_rn((float)x, o.x), d);
+      float w[3];
+      bool any = false;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const float wr = 1.0f - fabsf(__fsub_rn(tx, (float)(i0 + r)));
+        w[r] = (x >= xl[r] && x <= xh[r] && wr > 0.f) ? wr : 0.f;
+        any = any || w[r] > 0.f;
+      }
+      if (any) {
+        if (FILL) out[n] = make_int4(y * N + x, __float_as_int(w[0]), __float_as_int(w[1]), __float_as_int(w[2]));
+        ++n;
+      }
+    }
+  }
+  return n;
+}
+
+__global__ void k_run_count(const float4 *__restrict__ ofs, int N, int nd, int nang, int *__restrict__ count) {
+  const int nq = (nd + 2) / 3;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nq * nang) return;
+  const int j = t / nq, q = t - j * nq;
+  count[t] = run_walk<false>(__ldg(ofs + j), 3 * q, N, nd, nullptr);
+}
+
+__global__ void k_run_fill(const float4 *__restrict__ ofs, int N, int nd, int nang, const long long *__restrict__ start,
+                           int4 *__restrict__ ent) {
+  const int nq = (nd + 2) / 3;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nq * nang) return;
+  const int j = t / nq, q = t - j * nq;
+  run_walk<true>(__ldg(ofs + j), 3 * q, N, nd, ent + start[t]);
+}
+
 // acc += w * v per slice: the reference's separately rounded product and sum
 // (EXACT), or one fused multiply-add (the solver's hot loops)
 template <bool EXACT>
@@ -1876,6 +1951,82 @@ __global__ void __launch_bounds__(256) k_fwd_run(const IterParams P) {
   }
 }
 
+// k_fwd_rt: k_fwd over 3-bin runs from the run table (each pixel loaded once for
+// three bins), same fused data-term prox per bin.
+template <int DISC, int VW, int UNR>
+__global__ void __launch_bounds__(256) k_fwd_rt(const IterParams P) {
+  const Dims d = P.d;
+  const int nq = (d.nd + 2) / 3;
+  long long unit;
+  Slices<VW> sl;
+  if (!map_thread<VW>((long long)nq * d.nang, d.S, unit, sl)) return;
+  const int j = (int)(unit / nq), i0 = 3 * (int)(unit - (long long)j * nq);
+  float acc[3][VW];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < VW; ++k) acc[r][k] = 0.f;
+  const long long e0 = __ldg(P.run_start + unit), e1 = __ldg(P.run_start + unit + 1);
+  const int4 *ent = P.run_ent + e0;
+  const int n = (int)(e1 - e0);
+  int e = 0;
+  for (; e + UNR <= n; e += UNR) {
+    int4 en[UNR];
+    float v[UNR][VW];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) en[u] = __ldg(ent + e + u);
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) sl.load(P.ubar + (size_t)en[u].x * d.S, v[u]);
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const float w0 = __int_as_float(en[u].y), w1 = __int_as_float(en[u].z), w2 = __int_as_float(en[u].w);
+#pragma unroll
+      for (int k = 0; k < VW; ++k) {
+        acc[0][k] = __fmaf_rn(w0, v[u][k], acc[0][k]);
+        acc[1][k] = __fmaf_rn(w1, v[u][k], acc[1][k]);
+        acc[2][k] = __fmaf_rn(w2, v[u][k], acc[2][k]);
+      }
+    }
+  }
+  for (; e < n; ++e) {
+    const int4 en = __ldg(ent + e);
+    float v[VW];
+    sl.load(P.ubar + (size_t)en.x * d.S, v);
+    const float w0 = __int_as_float(en.y), w1 = __int_as_float(en.z), w2 = __int_as_float(en.w);
+#pragma unroll
+    for (int k = 0; k < VW; ++k) {
+      acc[0][k] = __fmaf_rn(w0, v[k], acc[0][k]);
+      acc[1][k] = __fmaf_rn(w1, v[k], acc[1][k]);
+      acc[2][k] = __fmaf_rn(w2, v[k], acc[2][k]);
+    }
+  }
+  const float sd = P.sigma_data;
+  float m[VW];
+#pragma unroll
+  for (int k = 0; k < VW; ++k) m[k] = sl.valid(k) ? __ldg(P.mu + sl.slice(k) / d.Nz) : 0.f;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    if (i0 + r >= d.nd) break;
+    const size_t q = ((size_t)j * d.nd + i0 + r) * d.S;
+    sl.store(P.ku + q, acc[r]);
+    float lam[VW], f[VW];
+    sl.loadw(P.lam + q, lam);
+    sl.load(P.f + q, f);
+#pragma unroll
+    for (int k = 0; k < VW; ++k) {
+      if (DISC == KL) {
+        const float sv = lam[k] + sd * acc[r][k];
+        const float wv = sv - m[k];
+        const float dv = wv * wv + 4.f * sd * f[k] * m[k];
+        lam[k] = sv - 0.5f * (wv + sqrtf(dv));
+      } else {
+        lam[k] = (lam[k] + sd * (acc[r][k] - f[k])) * m[k];
+      }
+    }
+    sl.store(P.lam + q, lam);
+  }
+}
+
 // slices per lane: 8 (two float4 chunks) when S is a multiple of 4, else 2, else 1
 static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 : 1); }
 
@@ -1889,13 +2040,14 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // (8, 2, on the fly), (4, 2, on the fly); configs 9..12 = (slices per lane,
 // pixels per run) of k_bp_run = (8, 4), (4, 8), (8, 8), (4, 4).  k_fwd config 9 and
 // k_bp config 13: one slice per lane with the 32-slice chunk outermost (SlicesWL),
-// for images and sinograms larger than L2.
+// for images and sinograms larger than L2.  k_fwd configs 10, 11: the 3-bin run
+// table (k_fwd_rt) with (slices per lane, entries in flight) = (8, 4), (4, 8).
 // Otherwise one fixed shape with 2 or 1 slices per thread.
 // One more candidate each: one slice per thread (k_fwd config 4, k_bp config 8),
 // which keeps all lanes busy when S is small.
 int num_proj_configs(int S, int which) {
   if (S % 4 != 0) return 1;
-  return which == 0 ? 10 : 14;  // configs 4 / 8 (one slice per thread) stay candidates for every S
+  return which == 0 ? 12 : 14;  // configs 4 / 8 (one slice per thread) stay candidates for every S
 }
 
 template <int VW, int UNR>
@@ -1903,6 +2055,14 @@ static void fwd_vw(const IterParams &P, int disc, cudaStream_t st) {
   const unsigned g = blocks_for(threads_for<VW>((long long)P.d.nd * P.d.nang, P.d.S), 256);
   if (disc == KL) k_fwd<KL, VW, UNR><<<g, 256, 0, st>>>(P);
   else k_fwd<L2, VW, UNR><<<g, 256, 0, st>>>(P);
+}
+
+template <int VW, int UNR>
+static void fwd_rt(const IterParams &P, int disc, cudaStream_t st) {
+  const long long units = (long long)((P.d.nd + 2) / 3) * P.d.nang;
+  const unsigned g = blocks_for(threads_for<VW>(units, P.d.S), 256);
+  if (disc == KL) k_fwd_rt<KL, VW, UNR><<<g, 256, 0, st>>>(P);
+  else k_fwd_rt<L2, VW, UNR><<<g, 256, 0, st>>>(P);
 }
 
 static void fwd_wl(const IterParams &P, int disc, cudaStream_t st) {
@@ -1933,6 +2093,12 @@ cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
       case 8: fwd_run<4, 8>(P, disc, st); break;
       case 9:
         if (P.ray_start) fwd_wl(P, disc, st); else fwd_vw<8, 4>(P, disc, st);  // WL streams the ray table
+        break;
+      case 10:
+        if (P.run_start) fwd_rt<8, 4>(P, disc, st); else fwd_vw<8, 4>(P, disc, st);
+        break;
+      case 11:
+        if (P.run_start) fwd_rt<4, 8>(P, disc, st); else fwd_vw<8, 4>(P, disc, st);
         break;
       default: fwd_vw<8, 4>(P, disc, st); break;
     }
@@ -2032,6 +2198,17 @@ cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, in
   if (vw == 8) k_radon_ad<8><<<blocks_for(threads_for<8>(units, S), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
   else if (vw == 2) k_radon_ad<2><<<blocks_for(threads_for<2>(units, S), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
   else k_radon_ad<1><<<blocks_for(threads_for<1>(units, S), 256), 256, 0, st>>>(sino, img, ofs, N, nd, nang, S);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_run_count(const float4 *ofs, int N, int nd, int nang, int *count, cudaStream_t st) {
+  k_run_count<<<blocks_for((long long)((nd + 2) / 3) * nang, 128), 128, 0, st>>>(ofs, N, nd, nang, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_run_fill(const float4 *ofs, int N, int nd, int nang, const long long *start, int4 *ent,
+                            cudaStream_t st) {
+  k_run_fill<<<blocks_for((long long)((nd + 2) / 3) * nang, 128), 128, 0, st>>>(ofs, N, nd, nang, start, ent);
   return cudaGetLastError();
 }
 

@@ -336,12 +336,13 @@ class WarmStarter:
     that the first iterations pull u back towards the cold-start state."""
 
     def __init__(self, net: UNet3D, fields=("u", "v"), pre_iters: int = 20, use=None, reset_dual: bool = True,
-                 empty_weight: float = 1.0, cap: int = 0, repair: bool = True):
+                 empty_weight: float = 1.0, cap: int = 0, repair: bool = True, use_network: bool = True):
         self.net, self.fields, self.pre_iters = net, tuple(fields), int(pre_iters)
         self.use = tuple(use) if use is not None else self.fields  # predicted fields written to the solver
         self.reset_dual = bool(reset_dual)
         self.empty_weight = float(empty_weight)  # fraction of the reset applied on bins without data
         self.repair = bool(repair)  # lift u along rays with data that the prediction misses
+        self.use_network = bool(use_network)  # False: the lambda reset alone (for comparisons)
         self.cap = int(cap)  # 0: keep lambda where f > 10 K u; 10 / 100: lambda = mu (1 - cap) there
         if self.fields[0] != "u":
             raise ValueError("the first predicted field must be u (the residual channels)")
@@ -410,9 +411,10 @@ class WarmStarter:
         _ck(lib.gt_get_state_device(prob._h, L.FIELDS["u"], _p(u)))
         _ck(lib.gt_nn_scale(_p(u), F32, _p(x), BF16, C, 1, vol, _p(inv), 0, st))
         _ck(lib.gt_nn_scale(_p(u), F32, _p(out), F32, C, 1, vol, _p(inv), 0, st))
-        net.forward(x, out, st)
+        if self.use_network:
+            net.forward(x, out, st)
         ch = 0
-        for fl in self.fields:
+        for fl in (self.fields if self.use_network else ()):
             n = FIELD_COMPS[fl] * C
             src = ctypes.c_void_p(out.data_ptr() + 4 * ch * vol)
             dst = ctypes.c_void_p(res.data_ptr() + 4 * ch * vol)
@@ -566,14 +568,15 @@ def iterations_to_gap(prob, tol: float, check_every: int = 100, max_iters: int =
 def evaluate(net: UNet3D, seeds, N, Nz, C=2, nang=71, mu=(0.2, 5e-4), alpha=(4.0, 1.0), fields=("u",),
              pre_iters=500, tol=1e-2, check_every=100, max_iters=40000, device=0, log=None):
     """Iterations and wall time to relative gap <= tol per held-out seed, for the
-    cold start, the dual reset alone (pre_iters cold iterations, then lambda from
-    K u, no network) and the warm start (pre_iters cold iterations, the network's
-    u, lambda from K u).  Also the relative distance of each final u to the cold
-    run's (the same minimiser)."""
+    cold start, the same procedure without the network (pre_iters cold
+    iterations, lambda from K u of that iterate, missed-ray lift at checks) and
+    the warm start (the same with the network's u).  Also the relative distance
+    of each final u to the cold run's (the same minimiser)."""
     import torch
 
     from .solver import Problem
     ws = WarmStarter(net, fields, pre_iters)
+    ws_reset = WarmStarter(net, fields, pre_iters, use_network=False)  # everything but the network
     rows = []
     for s in seeds:
         f, ang = phantom_case(s, N, Nz, C, nang, device=device)
@@ -588,10 +591,9 @@ def evaluate(net: UNet3D, seeds, N, Nz, C=2, nang=71, mu=(0.2, 5e-4), alpha=(4.0
                 fell_back = False
                 if mode == "warm":
                     it, g, fell_back = solve_warm(p, f, ws, tol, check_every, max_iters)
+                elif mode == "reset":
+                    it, g, fell_back = solve_warm(p, f, ws_reset, tol, check_every, max_iters)
                 else:
-                    if mode == "reset":
-                        p.run(pre_iters).dual_from_primal()
-                        extra = pre_iters
                     it, g = iterations_to_gap(p, tol, check_every, max_iters)
                 p.synchronize()
                 row[mode] = {"iterations": it + extra, "gap": g, "seconds": time.perf_counter() - t0}
