@@ -47,6 +47,7 @@ cudaError_t launch_run_fill(const float4 *ofs, int N, int nd, int nang, const lo
                             cudaStream_t st);
 int num_proj_configs(int S, int which);
 bool dual_z2_ok(const IterParams &P, int tgv, int cpl);
+int num_dual_configs(const IterParams &P);
 int gap_blocks(const IterParams &P);
 cudaError_t launch_gap_pass1(const IterParams &P, int disc, int tgv, int cpl, float *vt, double *part, int nb,
                              cudaStream_t st);
@@ -218,8 +219,7 @@ std::map<TuneKey, std::tuple<int, int, int>> g_tune;
 
 int autotune(gt_problem *p) {
   const bool tgv = p->reg == GT_TGV;
-  const int nc[3] = {gt::num_proj_configs(p->d.S, 0), gt::num_proj_configs(p->d.S, 1),
-                     gt::dual_z2_ok(p->P, tgv, p->cpl) ? 2 : 1};
+  const int nc[3] = {gt::num_proj_configs(p->d.S, 0), gt::num_proj_configs(p->d.S, 1), gt::num_dual_configs(p->P)};
   p->P.fwd_cfg = 0;
   p->P.bp_cfg = 0;
   p->P.dual_cfg = 0;
@@ -696,8 +696,9 @@ int gt_set_tuning(gt_problem *p, int fwd_cfg, int bp_cfg) {
 
 int gt_set_dual_shape(gt_problem *p, int cfg) {
   if (!p) return set_err(GT_ERR_ARG, "null argument");
-  const int n = gt::dual_z2_ok(p->P, p->reg == GT_TGV, p->cpl) ? 2 : 1;
-  if (cfg < 0 || cfg >= n) return set_err(GT_ERR_ARG, "dual launch shape %d out of range (%d available)", cfg, n);
+  const int n = gt::num_dual_configs(p->P);
+  if (cfg < 0 || cfg >= n || (cfg == 1 && !gt::dual_z2_ok(p->P, p->reg == GT_TGV, p->cpl)))
+    return set_err(GT_ERR_ARG, "dual launch shape %d not available here", cfg);
   CK(cudaSetDevice(p->device));
   CK(cudaStreamSynchronize(p->stream));
   p->P.dual_cfg = cfg;

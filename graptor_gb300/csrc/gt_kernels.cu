@@ -222,8 +222,8 @@ __device__ __forceinline__ float wnorm2(const float *w) {
 // 2-D :286-304), NormV / NormW (3-D :290-610, 2-D :98-258)
 // thread = one (pixel, z); it owns all C channels of that voxel.
 // ===========================================================================
-template <int DIM, bool TGV, int CPL, int CMAX>
-__global__ void __launch_bounds__(256) k_dual(const IterParams P) {
+template <int DIM, bool TGV, int CPL, int CMAX, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) k_dual(const IterParams P) {
   constexpr int K = DIM, KW = DIM == 3 ? 6 : 3;
   const Dims d = P.d;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -935,8 +935,8 @@ __device__ __forceinline__ void radon_table(const float *__restrict__ img, size_
 }
 
 // k_fwd: radon of ubar fused with update_lambda_KL (3-D :690-704) or _L2 (:677-688).
-template <int DISC, int VW, int UNR, bool WL = false>
-__global__ void __launch_bounds__(256) k_fwd(const IterParams P) {
+template <int DISC, int VW, int UNR, bool WL = false, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) k_fwd(const IterParams P) {
   const Dims d = P.d;
   long long unit;
   typename std::conditional<WL, SlicesWL, Slices<VW>>::type sl;
@@ -1800,6 +1800,10 @@ bool dual_z2_ok(const IterParams &P, int tgv, int cpl) {
   return P.d.dim == 3 && tgv && (cpl == FROB || cpl == UNCORR) && P.d.C <= 4 && P.d.Nz % 2 == 0;
 }
 
+// dual launch shapes: 0 k_dual, 1 k_dual_z2 (where dual_z2_ok; else the same as 0),
+// 2 k_dual with registers capped for 5 resident blocks (C <= 4; else as 0)
+int num_dual_configs(const IterParams &P) { return P.d.C <= 4 ? 3 : 1; }
+
 template <int CPL>
 static void launch_dual_z2(const IterParams &P, cudaStream_t st) {
   const unsigned g = blocks_for((long long)P.d.N * P.d.N * (P.d.Nz / 2), 256);
@@ -1816,6 +1820,12 @@ static cudaError_t launch_dual_c(const IterParams &P, cudaStream_t st) {
   const int C = P.d.C;
   if (DIM == 3 && TGV && CPL != NUCL && P.dual_cfg == 1 && C <= 4 && P.d.Nz % 2 == 0) {
     launch_dual_z2<CPL == NUCL ? FROB : CPL>(P, st);
+    return cudaGetLastError();
+  }
+  if (P.dual_cfg == 2 && C <= 4) {  // registers capped for 5 resident blocks
+    if (C <= 1) k_dual<DIM, TGV, CPL, 1, 5><<<g, 256, 0, st>>>(P);
+    else if (C <= 2) k_dual<DIM, TGV, CPL, 2, 5><<<g, 256, 0, st>>>(P);
+    else k_dual<DIM, TGV, CPL, 4, 5><<<g, 256, 0, st>>>(P);
     return cudaGetLastError();
   }
   if (C <= 1) k_dual<DIM, TGV, CPL, 1><<<g, 256, 0, st>>>(P);
@@ -2041,13 +2051,14 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // pixels per run) of k_bp_run = (8, 4), (4, 8), (8, 8), (4, 4).  k_fwd config 9 and
 // k_bp config 13: one slice per lane with the 32-slice chunk outermost (SlicesWL),
 // for images and sinograms larger than L2.  k_fwd configs 10, 11: the 3-bin run
-// table (k_fwd_rt) with (slices per lane, entries in flight) = (8, 4), (4, 8).
+// table (k_fwd_rt) with (slices per lane, entries in flight) = (8, 4), (4, 8);
+// configs 12, 13: (8, 8) and (8, 4) with registers capped for 5 / 6 resident blocks.
 // Otherwise one fixed shape with 2 or 1 slices per thread.
 // One more candidate each: one slice per thread (k_fwd config 4, k_bp config 8),
 // which keeps all lanes busy when S is small.
 int num_proj_configs(int S, int which) {
   if (S % 4 != 0) return 1;
-  return which == 0 ? 12 : 14;  // configs 4 / 8 (one slice per thread) stay candidates for every S
+  return which == 0 ? 14 : 14;  // configs 4 / 8 (one slice per thread) stay candidates for every S
 }
 
 template <int VW, int UNR>
@@ -2055,6 +2066,14 @@ static void fwd_vw(const IterParams &P, int disc, cudaStream_t st) {
   const unsigned g = blocks_for(threads_for<VW>((long long)P.d.nd * P.d.nang, P.d.S), 256);
   if (disc == KL) k_fwd<KL, VW, UNR><<<g, 256, 0, st>>>(P);
   else k_fwd<L2, VW, UNR><<<g, 256, 0, st>>>(P);
+}
+
+// the same with a register cap for MINB resident blocks of 256 per SM (occupancy)
+template <int VW, int UNR, int MINB>
+static void fwd_vw_occ(const IterParams &P, int disc, cudaStream_t st) {
+  const unsigned g = blocks_for(threads_for<VW>((long long)P.d.nd * P.d.nang, P.d.S), 256);
+  if (disc == KL) k_fwd<KL, VW, UNR, false, MINB><<<g, 256, 0, st>>>(P);
+  else k_fwd<L2, VW, UNR, false, MINB><<<g, 256, 0, st>>>(P);
 }
 
 template <int VW, int UNR>
@@ -2100,6 +2119,8 @@ cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
       case 11:
         if (P.run_start) fwd_rt<4, 8>(P, disc, st); else fwd_vw<8, 4>(P, disc, st);
         break;
+      case 12: fwd_vw_occ<8, 8, 5>(P, disc, st); break;
+      case 13: fwd_vw_occ<8, 4, 6>(P, disc, st); break;
       default: fwd_vw<8, 4>(P, disc, st); break;
     }
   } else if (S % 2 == 0) {

@@ -106,8 +106,9 @@ GT_API int gt_get_tuning(gt_problem *p, int out[2]);
 GT_API int gt_set_tuning(gt_problem *p, int fwd_cfg, int bp_cfg);
 /* Launch shape of the dual kernel: 0 = one slice per thread (every case),
  * 1 = two slices per thread with float2 accesses (3-D TGV, Frobenius or
- * uncorrelated coupling, C <= 4, Nz even).  Both give bit-identical iterates;
- * the autotuner picks the faster.  gt_get_dual_shape returns the current one. */
+ * uncorrelated coupling, C <= 4, Nz even), 2 = shape 0 with registers capped
+ * for 5 resident blocks per SM (C <= 4).  All give bit-identical iterates; the
+ * autotuner picks the fastest.  gt_get_dual_shape returns the current one. */
 GT_API int gt_set_dual_shape(gt_problem *p, int cfg);
 GT_API int gt_get_dual_shape(gt_problem *p);
 

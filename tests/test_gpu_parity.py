@@ -243,8 +243,8 @@ def test_projector_launch_shapes_give_identical_iterates(S_case):
 
 @pytest.mark.parametrize("C,cpl", [(1, "FROB"), (2, "FROB"), (3, "UNCORR"), (4, "FROB")])
 def test_dual_launch_shapes_give_identical_iterates(C, cpl):
-    """The two-slice float2 dual kernel computes every value with the same
-    operations as the one-slice kernel: identical iterates."""
+    """The two-slice float2 dual kernel and the register-capped one compute every
+    value with the same operations as the one-slice kernel: identical iterates."""
     from graptor_gb300 import phantom
     from graptor_gb300.solver import Problem
     N, Nz, nang = 28, 6, 15
@@ -253,15 +253,16 @@ def test_dual_launch_shapes_give_identical_iterates(C, cpl):
     f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
     got = []
     with Problem(3, N, Nz, C, N, ang, (4, 1), [0.3] * C, coupling=cpl, normest=17.0, stepsize=2.0) as p:
-        for shape in (0, 1):
+        for shape in (0, 1, 2):
             p.set_data(f)
             p.set_dual_shape(shape)
             p.run(9).synchronize()
             got.append({k: p.get(k) for k in ("u", "v", "w", "p")})
         with pytest.raises(ValueError):
-            p.set_dual_shape(2)
-    for k in got[0]:
-        np.testing.assert_array_equal(got[1][k], got[0][k], err_msg=k)
+            p.set_dual_shape(3)
+    for g in got[1:]:
+        for k in got[0]:
+            np.testing.assert_array_equal(g[k], got[0][k], err_msg=k)
     with Problem(3, N, 5, C, N, ang, (4, 1), [0.3] * C, normest=17.0) as q:  # odd Nz: one shape only
         with pytest.raises(ValueError):
             q.set_dual_shape(1)
