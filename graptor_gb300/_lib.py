@@ -46,6 +46,19 @@ class GtDesc(ctypes.Structure):
     ]
 
 
+class GtSubsDesc(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int), ("Nz", ctypes.c_int), ("C0", ctypes.c_int), ("C1", ctypes.c_int),
+        ("nang0", ctypes.c_int), ("nang1", ctypes.c_int), ("nd1", ctypes.c_int), ("Nz1", ctypes.c_int),
+        ("angles0", ctypes.POINTER(ctypes.c_double)), ("angles1", ctypes.POINTER(ctypes.c_double)),
+        ("stepsize", ctypes.c_float), ("alpha0", ctypes.c_double), ("alpha1", ctypes.c_double),
+        ("mu", ctypes.POINTER(ctypes.c_double)), ("discrepancy", ctypes.c_int), ("regularisation", ctypes.c_int),
+        ("coupling", ctypes.c_int), ("pixel_ratio", ctypes.c_double), ("refold", ctypes.c_double * 2),
+        ("refnew", ctypes.c_double * 2), ("normest", ctypes.c_double), ("device", ctypes.c_int),
+        ("stream", ctypes.c_void_p),
+    ]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _LL = ctypes.c_longlong
@@ -99,6 +112,13 @@ _SIGS = {
     "gt_nn_adam": (ctypes.c_int, [_P, _P, _P, _P, _P, _LL, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float, _I, _P]),
     "gt_nn_cast": (ctypes.c_int, [_P, _I, _P, _LL, _P]),
+    "gt_subs_create": (ctypes.c_int, [ctypes.POINTER(GtSubsDesc), ctypes.POINTER(ctypes.c_void_p)]),
+    "gt_subs_destroy": (None, [_P]),
+    "gt_subs_set_data": (ctypes.c_int, [_P, _P, _P, _I]),
+    "gt_subs_run": (ctypes.c_int, [_P, _I]),
+    "gt_subs_get": (ctypes.c_int, [_P, _I, _P]),
+    "gt_subs_normest": (ctypes.c_double, [_P]),
+    "gt_subs_problem": (ctypes.c_void_p, [_P]),
     "gt_last_error": (ctypes.c_char_p, []),
     "gt_version": (ctypes.c_char_p, []),
 }

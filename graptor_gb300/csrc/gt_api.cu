@@ -33,6 +33,14 @@ cudaError_t launch_feasible(float *f, const float *r1, int nbin1, int S, cudaStr
 cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
                                 int Nz, int disc, float empty_weight, float cap, cudaStream_t st);
 cudaError_t launch_missed_rays(const float *ku, const float *f, float *r, long long n, int N, cudaStream_t st);
+cudaError_t launch_gather_slices(const float *src, int S, int s0, float *dst, int Sg, long long X, cudaStream_t st);
+cudaError_t launch_scatter_slices(const float *src, int Sg, float *dst, int S, int s0, long long X, cudaStream_t st);
+cudaError_t launch_csr_planes(const float *in, float *out, const int *start, const int *idx, const float *val,
+                              int nang, int C, int nx_o, int nz_o, int nx_i, int nz_i, cudaStream_t st);
+cudaError_t launch_lambda_update(float *lam, const float *ku, const float *f, const float *mu, float sigma,
+                                 long long n, int S, int Nz, int disc, cudaStream_t st);
+cudaError_t launch_sumsq(const float *x, long long n, double *part, int nb, cudaStream_t st);
+cudaError_t launch_scale_f32(float *x, long long n, float s, cudaStream_t st);
 cudaError_t launch_add2(float *a, float *b, const float *d, long long n, cudaStream_t st);
 cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, double *d_img, double *d_sino,
                       double *d_part, double *out, cudaStream_t st);
@@ -135,6 +143,7 @@ struct gt_problem {
   int chunk = 16;
   long long iters = 0;
   bool has_data = false;
+  double lsqr = 0;             // > 0: step-size constant of a variant (two-resolution solver: 36)
 };
 
 namespace {
@@ -193,7 +202,7 @@ int field_info(gt_problem *p, int field, float **ptr, int *comps, size_t *X) {
 
 void set_scalars(gt_problem *p) {
   // tgv_radon :1178-1189 (3-D) / :753-762 (2-D)
-  const double Lsqr = p->d.dim == 3 ? 17.0 : 0.5 * (18.0 + std::sqrt(33.0));
+  const double Lsqr = p->lsqr > 0 ? p->lsqr : (p->d.dim == 3 ? 17.0 : 0.5 * (18.0 + std::sqrt(33.0)));
   p->sigma = 1.0 / std::sqrt(Lsqr);
   p->tau = p->sigma;
   const double ne2 = p->ne * p->ne;
@@ -1004,5 +1013,391 @@ int gt_batch_invalidate(gt_batch *b) {
   if (b->g_one) { cudaGraphExecDestroy(b->g_one); b->g_one = nullptr; }
   return GT_OK;
 }
+
+}  // extern "C"
+
+// ===========================================================================
+// Two-resolution subsampling (radon_tgv_primal_dual_3dsubsample.py:51-1240).
+// Channels [0, C0) have data at the image resolution (tilt series angles0);
+// channels [C0, C0+C1) have data of a coarser detector and slice grid (nd1 x Nz1,
+// tilt series angles1), related to the fine grid by an area-weighting matrix M
+// per angle and channel: their forward operator is M R1 and its adjoint R1^T M^T.
+// The regulariser couples all channels on the fine grid (k_dual / k_update of
+// the inner problem); step constant Lsqr = 36 (:1033-1036).
+// ===========================================================================
+namespace {
+
+// Create_Matrix_Line (3dsubsample :587-610): box of size a centred at (x, y) on
+// the fine grid, area weights a*b / (4 r0 r1), indices clipped to the grid.
+void matrix_line(const double a[2], double x, double y, int Nx, int Ny, std::vector<float> &A, std::vector<int> &I) {
+  const double r0 = a[0] / 2., r1 = a[1] / 2.;
+  const double xlower = x - r0, ylower = y - r1, xupper = x + r0, yupper = y + r1;
+  const int xli = (int)std::ceil(x - r0 - 0.499999), yli = (int)std::ceil(y - r1 - 0.499999);
+  const int xui = (int)std::floor(x + r0 + 0.499999), yui = (int)std::floor(y + r1 + 0.499999);
+  for (int j = yli; j <= yui; ++j)
+    for (int i = xli; i <= xui; ++i) {
+      const double a1 = std::max(std::min(xupper - i, 0.5), -0.5), a2 = std::max(std::min(i - xlower, 0.5), -0.5);
+      const double b1 = std::max(std::min(yupper - j, 0.5), -0.5), b2 = std::max(std::min(j - ylower, 0.5), -0.5);
+      const double v = (a1 + a2) * (b1 + b2) / (4. * r0 * r1);
+      const int ii = std::min(std::max(i, 0), Nx - 1), jj = std::min(std::max(j, 0), Ny - 1);
+      A.push_back((float)v);
+      I.push_back(ii + Nx * jj);
+    }
+}
+
+}  // namespace
+
+struct gt_subs {
+  gt_problem *p = nullptr;   // all channels on the fine grid
+  int C0 = 0, C1 = 0, Nz = 0, Nz1 = 0, nd1 = 0, nang0 = 0, nang1 = 0, N = 0;
+  int S0 = 0, S1 = 0, S1lo = 0;
+  int disc = GT_KL;
+  void *block = nullptr;
+  float4 *ofs0 = nullptr, *ofs1 = nullptr;
+  float *ub0 = nullptr, *ub1 = nullptr, *ks0 = nullptr, *ks1 = nullptr;
+  float *ku0 = nullptr, *ku1 = nullptr, *kulo = nullptr, *lamT = nullptr;
+  float *f0 = nullptr, *f1 = nullptr, *lam0 = nullptr, *lam1 = nullptr, *mu0 = nullptr, *mu1 = nullptr;
+  int *m_start = nullptr, *m_idx = nullptr, *mt_start = nullptr, *mt_idx = nullptr;
+  float *m_val = nullptr, *mt_val = nullptr;
+  double *part = nullptr;
+  cudaGraphExec_t g_one = nullptr, g_chunk = nullptr;
+  double normest = 0;
+  float sigma_data = 0;
+  bool has_data = false;
+};
+
+namespace {
+
+// the projector side of one iteration on the side stream: both data groups
+int subs_projections(gt_subs *s, cudaStream_t st) {
+  gt_problem *p = s->p;
+  const long long NN = (long long)s->N * s->N;
+  const int nd0 = s->N;
+  if (s->C0) {
+    CK(gt::launch_gather_slices(p->ubar, p->d.S, 0, s->ub0, s->S0, NN, st));
+    CK(gt::launch_radon(s->ub0, s->ku0, s->ofs0, s->N, nd0, s->nang0, s->S0, st));
+    CK(gt::launch_lambda_update(s->lam0, s->ku0, s->f0, s->mu0, s->sigma_data, (long long)s->nang0 * nd0 * s->S0,
+                                s->S0, s->Nz, s->disc, st));
+    CK(gt::launch_radon_ad(s->lam0, s->ks0, s->ofs0, s->N, nd0, s->nang0, s->S0, st));
+    CK(gt::launch_scatter_slices(s->ks0, s->S0, p->kstar, p->d.S, 0, NN, st));
+  }
+  CK(gt::launch_gather_slices(p->ubar, p->d.S, s->S0, s->ub1, s->S1, NN, st));
+  CK(gt::launch_radon(s->ub1, s->ku1, s->ofs1, s->N, nd0, s->nang1, s->S1, st));
+  CK(gt::launch_csr_planes(s->ku1, s->kulo, s->m_start, s->m_idx, s->m_val, s->nang1, s->C1, s->nd1, s->Nz1, nd0,
+                           s->Nz, st));
+  CK(gt::launch_lambda_update(s->lam1, s->kulo, s->f1, s->mu1, s->sigma_data, (long long)s->nang1 * s->nd1 * s->S1lo,
+                              s->S1lo, s->Nz1, s->disc, st));
+  CK(gt::launch_csr_planes(s->lam1, s->lamT, s->mt_start, s->mt_idx, s->mt_val, s->nang1, s->C1, nd0, s->Nz, s->nd1,
+                           s->Nz1, st));
+  CK(gt::launch_radon_ad(s->lamT, s->ks1, s->ofs1, s->N, nd0, s->nang1, s->S1, st));
+  CK(gt::launch_scatter_slices(s->ks1, s->S1, p->kstar, p->d.S, s->S0, NN, st));
+  return GT_OK;
+}
+
+int subs_iteration(gt_subs *s) {
+  gt_problem *p = s->p;
+  CK(cudaEventRecord(p->ev_fork, p->stream));
+  CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
+  int rc = subs_projections(s, p->side);
+  if (rc) return rc;
+  CK(gt::launch_dual(p->P, p->reg == GT_TGV, p->cpl, p->stream));
+  CK(cudaEventRecord(p->ev_join, p->side));
+  CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
+  CK(gt::launch_update(p->P, p->reg == GT_TGV, p->stream));
+  return GT_OK;
+}
+
+int subs_capture(gt_subs *s, int n, cudaGraphExec_t *out) {
+  gt_problem *p = s->p;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = GT_OK;
+  for (int k = 0; k < n && rc == GT_OK; ++k) rc = subs_iteration(s);
+  cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+  if (rc != GT_OK) { if (g) cudaGraphDestroy(g); return rc; }
+  if (e != cudaSuccess) return cuda_err(e, "cudaStreamEndCapture", __LINE__);
+  e = cudaGraphInstantiate(out, g, cudaGraphInstantiateFlagUseNodePriority);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_err(e, "cudaGraphInstantiate", __LINE__);
+  return GT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gt_subs_destroy(gt_subs *s) {
+  if (!s) return;
+  if (s->p) {
+    cudaSetDevice(s->p->device);
+    cudaStreamSynchronize(s->p->stream);
+  }
+  if (s->g_one) cudaGraphExecDestroy(s->g_one);
+  if (s->g_chunk) cudaGraphExecDestroy(s->g_chunk);
+  if (s->block) cudaFree(s->block);
+  if (s->p) gt_problem_destroy(s->p);
+  delete s;
+}
+
+int gt_subs_create(const gt_subs_desc *D, gt_subs **out) {
+  if (!D || !out) return set_err(GT_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (D->N < 1 || D->Nz < 1 || D->C0 < 0 || D->C1 < 1 || D->C0 + D->C1 > 8 || D->nang0 < (D->C0 ? 1 : 0) ||
+      D->nang1 < 1 || D->nd1 < 1 || D->Nz1 < 1 || !(D->pixel_ratio > 0) || !D->angles1 || (D->C0 && !D->angles0) ||
+      !D->mu || (D->coupling != GT_FROB && D->coupling != GT_UNCORR))
+    return set_err(GT_ERR_ARG, "gt_subs_create: invalid description");
+  gt_subs *s = new (std::nothrow) gt_subs();
+  if (!s) return set_err(GT_ERR_OOM, "host allocation failed");
+  s->C0 = D->C0; s->C1 = D->C1; s->Nz = D->Nz; s->Nz1 = D->Nz1; s->nd1 = D->nd1; s->N = D->N;
+  s->nang0 = D->nang0; s->nang1 = D->nang1; s->disc = D->discrepancy;
+  s->S0 = D->C0 * D->Nz; s->S1 = D->C1 * D->Nz; s->S1lo = D->C1 * D->Nz1;
+  // inner problem: the fine grid for every channel, regulariser and primal update
+  gt_desc d{};
+  d.dim = 3; d.N = D->N; d.Nz = D->Nz; d.C = D->C0 + D->C1; d.nd = D->N;
+  d.nang = D->C0 ? D->nang0 : D->nang1;
+  d.angles = D->C0 ? D->angles0 : D->angles1;
+  d.stepsize = D->stepsize; d.alpha0 = D->alpha0; d.alpha1 = D->alpha1; d.mu = D->mu;
+  d.discrepancy = D->discrepancy; d.regularisation = D->regularisation; d.coupling = D->coupling;
+  d.normest = 1.0; d.device = D->device; d.stream = D->stream; d.autotune = 0;
+  int rc = gt_problem_create(&d, &s->p);
+  if (rc) { delete s; return rc; }
+  s->p->lsqr = 36.0;
+  gt_problem *p = s->p;
+  cudaError_t e;
+  // interpolation matrix (Create_sparse_matrix :631-651 and its adjoint :612-629)
+  const int nd0 = D->N;
+  const double ratio[2] = {D->pixel_ratio, D->pixel_ratio / D->stepsize};
+  const double refnew1 = D->refnew[1] / D->stepsize;  // :945 (divides the caller's list in place there)
+  std::vector<int> start(1, 0), idx;
+  std::vector<float> val;
+  for (int j = 0; j < D->Nz1; ++j)
+    for (int i = 0; i < D->nd1; ++i) {
+      const double x = ratio[0] * (i - D->refold[0]) + D->refnew[0];
+      const double y = ratio[1] * (j - D->refold[1]) + refnew1;
+      matrix_line(ratio, x, y, nd0, D->Nz, val, idx);
+      start.push_back((int)idx.size());
+    }
+  // adjoint: for every fine node, the rows that reference it, in row order (one
+  // entry per reference, duplicates from clipping included)
+  const int nfine = nd0 * D->Nz, nrow = D->nd1 * D->Nz1;
+  std::vector<std::vector<int>> conn(nfine);
+  for (int r = 0; r < nrow; ++r)
+    for (int e2 = start[r]; e2 < start[r + 1]; ++e2) conn[idx[e2]].push_back(r);
+  std::vector<int> tstart(1, 0), tidx;
+  std::vector<float> tval;
+  {
+    std::vector<int> used(idx.size(), 0);
+    for (int i = 0; i < nfine; ++i) {
+      for (int r : conn[i]) {
+        for (int e2 = start[r]; e2 < start[r + 1]; ++e2)
+          if (idx[e2] == i && !used[e2]) { used[e2] = 1; tval.push_back(val[e2]); tidx.push_back(r); break; }
+      }
+      tstart.push_back((int)tidx.size());
+    }
+  }
+  // device block
+  const size_t NN = (size_t)D->N * D->N;
+  const size_t nb0 = (size_t)D->nang0 * nd0 * s->S0, nb1 = (size_t)D->nang1 * nd0 * s->S1,
+               nblo = (size_t)D->nang1 * D->nd1 * s->S1lo;
+  size_t off = 0;
+  auto take = [&](size_t bytes) { const size_t o = off; off += align256(std::max<size_t>(bytes, 4)); return o; };
+  const size_t o_ofs0 = take(16 * (size_t)std::max(D->nang0, 1)), o_ofs1 = take(16 * (size_t)D->nang1);
+  const size_t o_ub0 = take(4 * NN * s->S0), o_ub1 = take(4 * NN * s->S1);
+  const size_t o_ks0 = take(4 * NN * s->S0), o_ks1 = take(4 * NN * s->S1);
+  const size_t o_ku0 = take(4 * nb0), o_ku1 = take(4 * nb1), o_kulo = take(4 * nblo), o_lamT = take(4 * nb1);
+  const size_t o_f0 = take(4 * nb0), o_f1 = take(4 * nblo), o_lam0 = take(4 * nb0), o_lam1 = take(4 * nblo);
+  const size_t o_mu0 = take(4 * 8), o_mu1 = take(4 * 8);
+  const size_t o_ms = take(4 * start.size()), o_mi = take(4 * idx.size()), o_mv = take(4 * val.size());
+  const size_t o_ts = take(4 * tstart.size()), o_ti = take(4 * tidx.size()), o_tv = take(4 * tval.size());
+  const size_t o_part = take(8 * 256);
+  if ((e = cudaMalloc(&s->block, off)) != cudaSuccess) {
+    cudaGetLastError();
+    gt_subs_destroy(s);
+    return set_err(GT_ERR_OOM, "two-resolution buffers (%.3f GB)", off / 1e9);
+  }
+  char *b = (char *)s->block;
+  s->ofs0 = (float4 *)(b + o_ofs0); s->ofs1 = (float4 *)(b + o_ofs1);
+  s->ub0 = (float *)(b + o_ub0); s->ub1 = (float *)(b + o_ub1); s->ks0 = (float *)(b + o_ks0);
+  s->ks1 = (float *)(b + o_ks1); s->ku0 = (float *)(b + o_ku0); s->ku1 = (float *)(b + o_ku1);
+  s->kulo = (float *)(b + o_kulo); s->lamT = (float *)(b + o_lamT); s->f0 = (float *)(b + o_f0);
+  s->f1 = (float *)(b + o_f1); s->lam0 = (float *)(b + o_lam0); s->lam1 = (float *)(b + o_lam1);
+  s->mu0 = (float *)(b + o_mu0); s->mu1 = (float *)(b + o_mu1);
+  s->m_start = (int *)(b + o_ms); s->m_idx = (int *)(b + o_mi); s->m_val = (float *)(b + o_mv);
+  s->mt_start = (int *)(b + o_ts); s->mt_idx = (int *)(b + o_ti); s->mt_val = (float *)(b + o_tv);
+  s->part = (double *)(b + o_part);
+  // angle tables: both series on the fine detector (radon_struct with n_detectors = Nx0, :926-931)
+  auto table = [&](const double *ang, int nang, float4 *dst) -> int {
+    std::vector<double> t64;
+    angle_table(ang, D->N, nd0, nang, t64);
+    std::vector<float> t32(t64.size());
+    for (size_t k = 0; k < t64.size(); ++k) t32[k] = (float)t64[k];
+    CK(cudaMemcpyAsync(dst, t32.data(), 4 * t32.size(), cudaMemcpyHostToDevice, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    return GT_OK;
+  };
+  if (D->C0 && (rc = table(D->angles0, D->nang0, s->ofs0)) != GT_OK) { gt_subs_destroy(s); return rc; }
+  if ((rc = table(D->angles1, D->nang1, s->ofs1)) != GT_OK) { gt_subs_destroy(s); return rc; }
+  if ((e = cudaMemsetAsync(s->block, 0, o_ms, p->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(s->m_start, start.data(), 4 * start.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(s->m_idx, idx.data(), 4 * idx.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(s->m_val, val.data(), 4 * val.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(s->mt_start, tstart.data(), 4 * tstart.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(s->mt_idx, tidx.data(), 4 * tidx.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(s->mt_val, tval.data(), 4 * tval.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
+    gt_subs_destroy(s);
+    return cuda_err(e, "two-resolution set-up", __LINE__);
+  }
+  s->normest = D->normest;
+  *out = s;
+  return GT_OK;
+}
+
+// f0: [C0*Nz][nang0][N], f1: [C1*Nz1][nang1][nd1] (s = c*Nz + z); resets the iterates
+int gt_subs_set_data(gt_subs *s, const float *f0, const float *f1, int make_feasible) {
+  if (!s || (!f0 && s->C0) || !f1) return set_err(GT_ERR_ARG, "null argument");
+  gt_problem *p = s->p;
+  CK(cudaSetDevice(p->device));
+  const int nd0 = s->N;
+  const size_t nb0 = (size_t)s->nang0 * nd0 * s->S0, nblo = (size_t)s->nang1 * s->nd1 * s->S1lo;
+  // host layout [S][bins] -> device [bins][S]
+  if (s->C0) {
+    CK(cudaMemcpyAsync(p->stage, f0, 4 * nb0, cudaMemcpyHostToDevice, p->stream));
+    CK(gt::launch_transpose(p->stage, s->f0, s->S0, s->nang0 * nd0, p->stream));
+  }
+  CK(cudaMemcpyAsync(p->stage, f1, 4 * nblo, cudaMemcpyHostToDevice, p->stream));
+  CK(gt::launch_transpose(p->stage, s->f1, s->S1lo, s->nang1 * s->nd1, p->stream));
+  if (make_feasible) {
+    // Make_function_feasible (3dsubsample :466-476): bins where the projection of the
+    // all-ones slice is <= 0 are zeroed (the low-resolution data uses the mask of the
+    // fine detector, restricted to its own bins)
+    float *ones = p->stage, *r1 = p->ku;
+    CK(gt::fill_f32(ones, (size_t)s->N * s->N, 1.f, p->stream));
+    if (s->C0) {
+      CK(gt::launch_radon(ones, r1, s->ofs0, s->N, nd0, s->nang0, 1, p->stream));
+      CK(gt::launch_feasible(s->f0, r1, s->nang0 * nd0, s->S0, p->stream));
+    }
+    CK(gt::launch_radon(ones, r1, s->ofs1, s->N, nd0, s->nang1, 1, p->stream));
+    std::vector<float> mask((size_t)s->nang1 * nd0);
+    CK(cudaMemcpyAsync(mask.data(), r1, 4 * mask.size(), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    std::vector<float> m1((size_t)s->nang1 * s->nd1, 1.f);
+    for (int j = 0; j < s->nang1; ++j)
+      for (int i = 0; i < std::min(nd0, s->nd1); ++i)
+        if (mask[(size_t)j * nd0 + i] <= 0.f) m1[(size_t)j * s->nd1 + i] = 0.f;
+    CK(cudaMemcpyAsync(r1, m1.data(), 4 * m1.size(), cudaMemcpyHostToDevice, p->stream));
+    CK(gt::launch_feasible(s->f1, r1, s->nang1 * s->nd1, s->S1lo, p->stream));
+  }
+  // operator norm: injected, or a power iteration of K^T K from the all-ones image
+  if (!(s->normest > 0)) {
+    const long long n = (long long)p->d.vol;
+    float *x = p->u;
+    CK(gt::fill_f32(x, (size_t)n, 1.f, p->stream));
+    double nrm = 0;
+    std::vector<double> h(256);
+    gt_problem *pp = p;
+    for (int r = 0; r < 30; ++r) {
+      CK(gt::launch_sumsq(x, n, s->part, 256, pp->stream));
+      CK(cudaMemcpyAsync(h.data(), s->part, 8 * 256, cudaMemcpyDeviceToHost, pp->stream));
+      CK(cudaStreamSynchronize(pp->stream));
+      double a = 0;
+      for (double v : h) a += v;
+      nrm = std::sqrt(a);
+      if (!(nrm > 0)) return set_err(GT_ERR_CUDA, "two-resolution operator norm estimate failed");
+      CK(gt::launch_scale_f32(x, n, (float)(1.0 / nrm), pp->stream));
+      // x <- K^T K x, per group (ubar is the projections' input)
+      CK(cudaMemcpyAsync(p->ubar, x, 4 * (size_t)n, cudaMemcpyDeviceToDevice, pp->stream));
+      const long long NN = (long long)s->N * s->N;
+      if (s->C0) {
+        CK(gt::launch_gather_slices(p->ubar, p->d.S, 0, s->ub0, s->S0, NN, pp->stream));
+        CK(gt::launch_radon(s->ub0, s->ku0, s->ofs0, s->N, nd0, s->nang0, s->S0, pp->stream));
+        CK(gt::launch_radon_ad(s->ku0, s->ks0, s->ofs0, s->N, nd0, s->nang0, s->S0, pp->stream));
+        CK(gt::launch_scatter_slices(s->ks0, s->S0, x, p->d.S, 0, NN, pp->stream));
+      }
+      CK(gt::launch_gather_slices(p->ubar, p->d.S, s->S0, s->ub1, s->S1, NN, pp->stream));
+      CK(gt::launch_radon(s->ub1, s->ku1, s->ofs1, s->N, nd0, s->nang1, s->S1, pp->stream));
+      CK(gt::launch_csr_planes(s->ku1, s->kulo, s->m_start, s->m_idx, s->m_val, s->nang1, s->C1, s->nd1, s->Nz1, nd0,
+                               s->Nz, pp->stream));
+      CK(gt::launch_csr_planes(s->kulo, s->lamT, s->mt_start, s->mt_idx, s->mt_val, s->nang1, s->C1, nd0, s->Nz,
+                               s->nd1, s->Nz1, pp->stream));
+      CK(gt::launch_radon_ad(s->lamT, s->ks1, s->ofs1, s->N, nd0, s->nang1, s->S1, pp->stream));
+      CK(gt::launch_scatter_slices(s->ks1, s->S1, x, p->d.S, s->S0, NN, pp->stream));
+    }
+    s->normest = std::sqrt(nrm);
+  }
+  p->ne = s->normest;
+  set_scalars(p);
+  s->sigma_data = p->P.sigma_data;
+  // channel weights: KL mu, L2 mu/(sigma+mu) (:1038-1045)
+  std::vector<float> me(8, 0.f);
+  const int C = s->C0 + s->C1;
+  for (int c = 0; c < C; ++c)
+    me[c] = (float)(s->disc == GT_KL ? p->mu[c] : p->mu[c] / (p->sigma + p->mu[c]));
+  CK(cudaMemcpyAsync(s->mu0, me.data(), 4 * 8, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(s->mu1, me.data() + s->C0, 4 * (8 - s->C0), cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(p->mu_eff, me.data(), 4 * C, cudaMemcpyHostToDevice, p->stream));
+  p->P.ne64 = p->ne;
+  // zero the iterates (:1057-1075)
+  const size_t fv = 4 * p->d.vol;
+  CK(cudaMemsetAsync(p->u, 0, fv, p->stream));
+  CK(cudaMemsetAsync(p->ubar, 0, fv, p->stream));
+  if (p->p) CK(cudaMemsetAsync(p->p, 0, fv * p->K, p->stream));
+  if (p->pbar) CK(cudaMemsetAsync(p->pbar, 0, fv * p->K, p->stream));
+  CK(cudaMemsetAsync(p->v, 0, fv * p->K, p->stream));
+  if (p->w) CK(cudaMemsetAsync(p->w, 0, fv * p->KW, p->stream));
+  if (s->C0) CK(cudaMemsetAsync(s->lam0, 0, 4 * nb0, p->stream));
+  CK(cudaMemsetAsync(s->lam1, 0, 4 * nblo, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  if (s->g_one) { cudaGraphExecDestroy(s->g_one); s->g_one = nullptr; }
+  if (s->g_chunk) { cudaGraphExecDestroy(s->g_chunk); s->g_chunk = nullptr; }
+  p->iters = 0;
+  p->has_data = true;
+  s->has_data = true;
+  return GT_OK;
+}
+
+int gt_subs_run(gt_subs *s, int iters) {
+  if (!s) return set_err(GT_ERR_ARG, "null argument");
+  if (!s->has_data) return set_err(GT_ERR_STATE, "gt_subs_run before gt_subs_set_data");
+  if (iters <= 0) return iters == 0 ? GT_OK : set_err(GT_ERR_ARG, "negative iteration count");
+  gt_problem *p = s->p;
+  CK(cudaSetDevice(p->device));
+  int rc;
+  const int chunk = 16;
+  if (iters >= chunk && !s->g_chunk && (rc = subs_capture(s, chunk, &s->g_chunk)) != GT_OK) return rc;
+  if (!s->g_one && (rc = subs_capture(s, 1, &s->g_one)) != GT_OK) return rc;
+  int left = iters;
+  while (left >= chunk) { CK(cudaGraphLaunch(s->g_chunk, p->stream)); left -= chunk; }
+  while (left > 0) { CK(cudaGraphLaunch(s->g_one, p->stream)); --left; }
+  p->iters += iters;
+  return GT_OK;
+}
+
+// which: GT_SUBS_U [C*Nz][N][N]; GT_SUBS_KU0 [C0*Nz][nang0][N]; GT_SUBS_KU1 [C1*Nz][nang1][N]
+// (fine grid); GT_SUBS_KULO [C1*Nz1][nang1][nd1]
+int gt_subs_get(gt_subs *s, int which, float *host) {
+  if (!s || !host) return set_err(GT_ERR_ARG, "null argument");
+  gt_problem *p = s->p;
+  CK(cudaSetDevice(p->device));
+  CK(cudaStreamSynchronize(p->stream));
+  const int nd0 = s->N;
+  const float *src; int rows, cols;
+  switch (which) {
+    case GT_SUBS_U: return gt_get_state(p, GT_U, host);
+    case GT_SUBS_KU0: src = s->ku0; rows = s->nang0 * nd0; cols = s->S0; break;
+    case GT_SUBS_KU1: src = s->ku1; rows = s->nang1 * nd0; cols = s->S1; break;
+    case GT_SUBS_KULO: src = s->kulo; rows = s->nang1 * s->nd1; cols = s->S1lo; break;
+    default: return set_err(GT_ERR_ARG, "unknown field %d", which);
+  }
+  if (cols == 0) return GT_OK;
+  CK(gt::launch_transpose(src, p->stage, rows, cols, p->stream));
+  CK(cudaMemcpyAsync(host, p->stage, 4 * (size_t)rows * cols, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  return GT_OK;
+}
+
+double gt_subs_normest(const gt_subs *s) { return s ? s->normest : 0.0; }
+
+gt_problem *gt_subs_problem(gt_subs *s) { return s ? s->p : nullptr; }
 
 }  // extern "C"

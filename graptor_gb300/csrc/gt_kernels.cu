@@ -1467,6 +1467,116 @@ cudaError_t launch_add2(float *a, float *b, const float *d, long long n, cudaStr
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// two-resolution subsampling (radon_tgv_primal_dual_3dsubsample.py)
+// ---------------------------------------------------------------------------
+// slices [s0, s0 + Sg) of a [X][S] field <-> a contiguous [X][Sg] field
+__global__ void k_gather_slices(const float *__restrict__ src, int S, int s0, float *__restrict__ dst, int Sg,
+                                long long X) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= X * Sg) return;
+  const long long x = t / Sg;
+  dst[t] = src[x * S + s0 + (t - x * Sg)];
+}
+
+__global__ void k_scatter_slices(const float *__restrict__ src, int Sg, float *__restrict__ dst, int S, int s0,
+                                 long long X) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= X * Sg) return;
+  const long long x = t / Sg;
+  dst[x * S + s0 + (t - x * Sg)] = src[t];
+}
+
+// Sparsemultiplication (3dsubsample :403-428): for every angle j and channel c,
+// out(x_o, z_o) = sum over the row (x_o + nx_o z_o) of the interpolation matrix of
+// val * in(x_i, z_i), the column index being x_i + nx_i z_i; separately rounded
+// products summed in entry order.  Layouts [(j nx + x)][c nz + z].
+__global__ void k_csr_planes(const float *__restrict__ in, float *__restrict__ out, const int *__restrict__ start,
+                             const int *__restrict__ idx, const float *__restrict__ val, int nang, int C, int nx_o,
+                             int nz_o, int nx_i, int nz_i) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int So = C * nz_o, Si = C * nz_i;
+  if (t >= (long long)nang * nx_o * So) return;
+  const int s = (int)(t % So);
+  const long long jx = t / So;
+  const int x = (int)(jx % nx_o), j = (int)(jx / nx_o);
+  const int c = s / nz_o, z = s - c * nz_o;
+  const int row = x + nx_o * z;
+  float sum = 0.f;
+  for (int e = start[row]; e < start[row + 1]; ++e) {
+    const int k1 = idx[e];
+    const int zi = k1 / nx_i, xi = k1 - zi * nx_i;
+    sum = __fadd_rn(sum, __fmul_rn(val[e], in[((size_t)j * nx_i + xi) * Si + c * nz_i + zi]));
+  }
+  out[t] = sum;
+}
+
+// update_lambda_KL / _L2 (3-D :677-704) on a sinogram [bins][S], channel s / Nz
+__global__ void k_lambda_update(float *__restrict__ lam, const float *__restrict__ ku, const float *__restrict__ f,
+                                const float *__restrict__ mu, float sigma, long long n, int S, int Nz, int disc) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const float m = mu[(int)(t % S) / Nz];
+  if (disc == 0) {
+    const float sv = lam[t] + sigma * ku[t];
+    const float wv = sv - m;
+    const float dv = wv * wv + 4 * sigma * f[t] * m;
+    lam[t] = sv - 0.5f * (wv + sqrtf(dv));
+  } else {
+    lam[t] = (lam[t] + sigma * (ku[t] - f[t])) * m;
+  }
+}
+
+// sum of squares in FP64, block partials
+__global__ void k_sumsq_partial(const float *__restrict__ x, long long n, double *__restrict__ part) {
+  __shared__ double sh[256];
+  double a = 0.0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const double v = x[k];
+    a += v * v;
+  }
+  sh[threadIdx.x] = a;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_scale_f32(float *__restrict__ x, long long n, float s) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) x[t] *= s;
+}
+
+cudaError_t launch_gather_slices(const float *src, int S, int s0, float *dst, int Sg, long long X, cudaStream_t st) {
+  k_gather_slices<<<(unsigned)((X * Sg + 255) / 256), 256, 0, st>>>(src, S, s0, dst, Sg, X);
+  return cudaGetLastError();
+}
+cudaError_t launch_scatter_slices(const float *src, int Sg, float *dst, int S, int s0, long long X, cudaStream_t st) {
+  k_scatter_slices<<<(unsigned)((X * Sg + 255) / 256), 256, 0, st>>>(src, Sg, dst, S, s0, X);
+  return cudaGetLastError();
+}
+cudaError_t launch_csr_planes(const float *in, float *out, const int *start, const int *idx, const float *val,
+                              int nang, int C, int nx_o, int nz_o, int nx_i, int nz_i, cudaStream_t st) {
+  k_csr_planes<<<(unsigned)(((long long)nang * nx_o * C * nz_o + 255) / 256), 256, 0, st>>>(in, out, start, idx, val, nang, C,
+                                                                                  nx_o, nz_o, nx_i, nz_i);
+  return cudaGetLastError();
+}
+cudaError_t launch_lambda_update(float *lam, const float *ku, const float *f, const float *mu, float sigma,
+                                 long long n, int S, int Nz, int disc, cudaStream_t st) {
+  k_lambda_update<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(lam, ku, f, mu, sigma, n, S, Nz, disc);
+  return cudaGetLastError();
+}
+cudaError_t launch_sumsq(const float *x, long long n, double *part, int nb, cudaStream_t st) {
+  k_sumsq_partial<<<nb, 256, 0, st>>>(x, n, part);
+  return cudaGetLastError();
+}
+cudaError_t launch_scale_f32(float *x, long long n, float s, cudaStream_t st) {
+  k_scale_f32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, n, s);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
                                 int Nz, int disc, float empty_weight, float cap, cudaStream_t st) {
   k_lambda_fixed<<<(unsigned)((nbin * S + 255) / 256), 256, 0, st>>>(lam, ku, f, mu, nbin, S, Nz, disc, empty_weight,

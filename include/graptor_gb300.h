@@ -267,6 +267,44 @@ GT_API int gt_dual_from_primal_ex(gt_problem *p, int flags, float empty_weight);
 /* The problem's CUDA stream (the one gt_desc.stream named, or its own). */
 GT_API void *gt_problem_stream(gt_problem *p);
 
+/* Two-resolution subsampling: Reconstructionapproach3dsubsmapling
+ * (radon_tgv_primal_dual_3dsubsample.py:51).  Channels [0, C0) have sinograms on
+ * the image's own detector (N bins, Nz slices, tilt series angles0); channels
+ * [C0, C0+C1) have sinograms on a coarser grid (nd1 bins, Nz1 slices, tilt series
+ * angles1) related to the fine grid by the reference's area-weighting matrix
+ * (Create_sparse_matrix :631-651) built from pixel_ratio, refold, refnew and
+ * stepsize.  The TGV regulariser couples all channels on the fine grid. */
+typedef struct gt_subs gt_subs;
+typedef struct gt_subs_desc {
+  int N, Nz;            /* fine image N x N x Nz (detectors N) */
+  int C0, C1;           /* channels with fine / coarse data (C0 + C1 <= 8, C1 >= 1) */
+  int nang0, nang1;     /* angles of the two tilt series */
+  int nd1, Nz1;         /* coarse detector bins and slices */
+  const double *angles0, *angles1; /* radians, +pi/2 as the reference's callers pass them */
+  float stepsize;
+  double alpha0, alpha1;
+  const double *mu;     /* [C0 + C1] */
+  int discrepancy, regularisation, coupling;  /* coupling: GT_FROB or GT_UNCORR */
+  double pixel_ratio;   /* coarse pixel size / fine pixel size (Topology p) */
+  double refold[2];     /* reference point on the coarse grid (x, z) */
+  double refnew[2];     /* the same point on the fine grid (x, z) */
+  double normest;       /* > 0 used as given, else a power iteration from the all-ones image */
+  int device;
+  void *stream;
+} gt_subs_desc;
+enum { GT_SUBS_U = 0, GT_SUBS_KU0 = 1, GT_SUBS_KU1 = 2, GT_SUBS_KULO = 3 };
+GT_API int gt_subs_create(const gt_subs_desc *d, gt_subs **out);
+GT_API void gt_subs_destroy(gt_subs *s);
+/* f0 [C0*Nz][nang0][N], f1 [C1*Nz1][nang1][nd1] (s = c*Nz + z); resets the iterates */
+GT_API int gt_subs_set_data(gt_subs *s, const float *f0, const float *f1, int make_feasible);
+GT_API int gt_subs_run(gt_subs *s, int iters);
+/* GT_SUBS_U [(C0+C1)*Nz][N][N]; GT_SUBS_KU0 [C0*Nz][nang0][N]; GT_SUBS_KU1 [C1*Nz][nang1][N];
+ * GT_SUBS_KULO [C1*Nz1][nang1][nd1] (the last iteration's projections) */
+GT_API int gt_subs_get(gt_subs *s, int which, float *host);
+GT_API double gt_subs_normest(const gt_subs *s);
+/* the inner fine-grid problem (for gt_get_state / gt_set_state of the iterates) */
+GT_API gt_problem *gt_subs_problem(gt_subs *s);
+
 /* Number of kernel launches one iteration issues (for launch accounting). */
 GT_API int gt_launches_per_iteration(const gt_problem *p);
 

@@ -70,6 +70,12 @@ class Array:
         self._a *= self._a.dtype.type(other)
         return self
 
+    def __pow__(self, other):
+        # elementwise power in the array's type (the subsampling solver's norm, U_**2)
+        out = self._a ** self._a.dtype.type(other)
+        order = "F" if (self._a.flags.f_contiguous and not self._a.flags.c_contiguous) else "C"
+        return Array(self.queue, out.shape, out.dtype, order, host=np.asarray(out, order=order))
+
 
 def to_device(queue, ary, *_, **__):
     a = np.asarray(ary)

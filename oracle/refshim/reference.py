@@ -104,3 +104,34 @@ def run_3d(sino, angles, alpha, mu, maxiter, stepsize=1, discrepancy="KL",
             cl.Context(), [0, 0.1], int(stepsize), discrepancy, method, regularisation, [0.0, 1.0, [0]])
     (u, sinos), ne, ofs = _run(mod.Reconstructionapproach3d, args, seed)
     return np.asarray(u), np.asarray(sinos), ne, ofs
+
+
+def run_subs(sino, angles, topology, alpha, mu, maxiter, stepsize=1, discrepancy="KL",
+             method="Frobenius 3D Subsampling Reconstruction", regularisation="TGV", seed=0):
+    """Reference ``Reconstructionapproach3dsubsmapling``
+    (radon_tgv_primal_dual_3dsubsample.py:51); returns (Solution, [Sinograms0,
+    Sinograms1 fine, Sinograms1 coarse], normest).
+
+    The module does ``from numpy import *``, which shadows the built-in ``min`` /
+    ``max`` that its matrix construction (Create_Matrix_Line :587-610) calls with
+    two scalars; on current NumPy that raises.  The harness restores the built-ins
+    in the module's namespace (the code itself is unchanged).  The operator-norm
+    estimate is sqrt(sqrt(sum U^2)) of the last power-iteration round (:551, :575)."""
+    import builtins
+    mod = load("3dsubsample")
+    mod.min, mod.max = builtins.min, builtins.max
+    import pyopencl as cl
+    topo = [int(topology[0]), float(topology[1]), list(topology[2]), list(topology[3])]
+    args = (list(sino), list(angles), topo, tuple(alpha), np.asarray(mu, dtype=np.float64), int(maxiter),
+            cl.Context(), [0, 0.1], int(stepsize), discrepancy, method, regularisation, [0.0, 1.0, [0]])
+    _ensure_path()
+    cl.SUM_LOG.clear()
+    cl.COPY_LOG.clear()
+    np.random.seed(seed)
+    import io
+    import contextlib
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        u, sinos = mod.Reconstructionapproach3dsubsmapling(*args)
+    ne = math.sqrt(math.sqrt(cl.SUM_LOG[-1]))
+    return np.asarray(u), [np.asarray(x) for x in sinos], ne
