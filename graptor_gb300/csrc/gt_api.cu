@@ -1235,10 +1235,14 @@ int gt_subs_create(const gt_subs_desc *D, gt_subs **out) {
     CK(cudaStreamSynchronize(p->stream));
     return GT_OK;
   };
+  // zero the buffers first, then upload the tables into the block
+  if ((e = cudaMemsetAsync(s->block, 0, o_ms, p->stream)) != cudaSuccess) {
+    gt_subs_destroy(s);
+    return cuda_err(e, "two-resolution set-up", __LINE__);
+  }
   if (D->C0 && (rc = table(D->angles0, D->nang0, s->ofs0)) != GT_OK) { gt_subs_destroy(s); return rc; }
   if ((rc = table(D->angles1, D->nang1, s->ofs1)) != GT_OK) { gt_subs_destroy(s); return rc; }
-  if ((e = cudaMemsetAsync(s->block, 0, o_ms, p->stream)) != cudaSuccess ||
-      (e = cudaMemcpyAsync(s->m_start, start.data(), 4 * start.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
+  if ((e = cudaMemcpyAsync(s->m_start, start.data(), 4 * start.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
       (e = cudaMemcpyAsync(s->m_idx, idx.data(), 4 * idx.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
       (e = cudaMemcpyAsync(s->m_val, val.data(), 4 * val.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
       (e = cudaMemcpyAsync(s->mt_start, tstart.data(), 4 * tstart.size(), cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||

@@ -34,7 +34,7 @@ def test_subsampling_matches_reference(golden, name, parity_report):
                                                        normest=float(g[f"normest_{iters}"]))
         errs = {"u": rel(u, g[f"u_{iters}"]), "ku0": rel(sinos[0], g[f"ku0_{iters}"]),
                 "ku1": rel(sinos[1], g[f"ku1_{iters}"]), "kulo": rel(sinos[2], g[f"kulo_{iters}"])}
-        parity_report(f"subsampling {name} {iters} it", errs)
+        parity_report({"case": f"subsampling {name}", "iterations": iters, **errs})
         assert u.shape == g[f"u_{iters}"].shape
         for k, e in errs.items():
             assert e <= tol, (name, iters, k, e)
