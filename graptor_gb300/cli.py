@@ -15,12 +15,14 @@ MRC output (``<prefix>_<channel>.mrc``, ``_sinogram.mrc``, ``_all_channels.mrc``
 
 Differences: ``--GPU_Choice -1`` (the reference asks interactively) selects CUDA
 device 0; live plotting is not supported (``--Plot`` is accepted and ignored);
-the two-resolution subsampling couplings (FrobSubs / UncorrSubs) are not built
-and stop with an error; HDF5 input needs ``h5py``.
+HDF5 input needs ``h5py``.  The two-resolution couplings (FrobSubs / UncorrSubs)
+run ``Coupled_Reconstruction3dbigresu`` (:542-873) through the drop-in
+``Reconstructionapproach3dsubsmapling``.
 """
 from __future__ import annotations
 
 import argparse
+import math
 import os
 import sys
 import time
@@ -244,6 +246,180 @@ def reconstruct_3d(names, result, mu, alpha, maxiter, method, levels, datahandli
     return U
 
 
+def pixel_ratio(sizes, C0, given):
+    """Coarse/fine pixel ratio p (Reconstruction_coupled.py:590-611): from the pixel
+    sizes stored with the data when both resolutions have one (a different
+    ``--Pixelratio`` then aborts), else the ``--Pixelratio`` input; sizes within one
+    resolution must agree."""
+    jj = sizes.index(max(sizes[:C0]))
+    for i in range(C0):
+        if sizes[i] != sizes[jj] and sizes[i] > 0 and sizes[jj] > 0:
+            raise ValueError(f"Warning: no uniform Pixelsize in the high resolution data with sizes {sizes[i]} and "
+                             f"{sizes[jj]}. Aborting computations.")
+    j = sizes.index(max(sizes[C0:]))
+    if sizes[j] > 0 and sizes[jj] > 0:
+        p = sizes[j] / sizes[jj]
+        if abs(p - given) > 0.001 and given > 0:
+            raise ValueError(f"Warning: the Pixelratio given as input ({given}) does not coincide with the pixel ratio "
+                             f"obtained in the data({p}). Aborting computations.")
+        return p
+    if given > 0:
+        return given
+    raise ValueError("Warning: no suitable information concerning Pixelsize was given in input or in data. Aborting "
+                     "computations.")
+
+
+def coarse_section(levels_lo, levels_hi, p, refnew_y, refold_y, ny1, rounding):
+    """Coarse slices covering fine slices [levels_lo, levels_hi]: the fine slice index
+    mapped through the common centre, y1 = (y0 - refnew_y)/p + refold_y, clipped to
+    [0, ny1-1]; the whole section uses floor/ceil (:619-621), each chunk round (:715-717)."""
+    lo_f, hi_f = (math.floor, math.ceil) if rounding == "cover" else (round, round)
+    z_ = int(np.clip(lo_f(1 / p * (levels_lo - refnew_y) + refold_y), 0, ny1 - 1))
+    zu = int(np.clip(hi_f(1 / p * (levels_hi - refnew_y) + refold_y), 0, ny1 - 1))
+    return z_, zu
+
+
+def reconstruct_subs(names, C0, result, mu, alpha, maxiter, method, levels, datahandling, badprojections, find_bad,
+                     channelnames, regularisation, discrepancy, pixelratio, overlay, chunksize, scalepars, device=0):
+    """Joint reconstruction from fine (``names[:C0]``) and coarse (``names[C0:]``)
+    projection data (Coupled_Reconstruction3dbigresu, Reconstruction_coupled.py:542-873).
+
+    Per resolution its own data handling (``datahandling[k][r]``, r = 0 fine, 1 coarse)
+    and bad projections; the coarse/fine pixel ratio from the data or ``--Pixelratio``;
+    the fine slices ``levels`` and the coarse slices that cover them; slice chunks with
+    overlap, each reconstructed by the drop-in ``Reconstructionapproach3dsubsmapling``
+    (CUDA); per-channel rescaling by the data/sinogram ratio; MRC outputs (fine
+    reconstruction of every channel, fine sinograms, and for the coarse channels the
+    coarse ``_sinogram_smallresu.mrc`` and fine-grid ``_sinogram.mrc`` projections).
+
+    As in the reference, bad projections found by ``--Find_Bad_Projections`` are not
+    applied here (the reference appends them as a third, unread entry of the
+    per-resolution list), and the coarse channels' fine-grid sinograms are all divided
+    by the last coarse channel's factor."""
+    from .radon_tgv_primal_dual_3dsubsample import Reconstructionapproach3dsubsmapling
+    brightness, baseline, cutedges, badfile, threshold = datahandling[:5]
+    C = len(names)
+    C1 = C - C0
+    if C0 < 1 or C1 < 1:
+        raise ValueError("subsampling needs at least one fine and one coarse channel")
+    if find_bad[0] not in (0, 0.0):
+        eprint("Warning: bad projections found by --Find_Bad_Projections are not applied in the subsampling "
+               "reconstruction.")
+    data, angles, noise, sizes = [], [], [], []
+    for n in names:
+        r = int(n in names[C0:])
+        d, a, avg = preprocess.load_channel(n, brightness[r], badfile[r], float(cutedges[r]), badprojections[r])
+        data.append(d)
+        angles.append(np.asarray(a, np.float64) + np.pi / 2)
+        noise.append(avg)
+        sizes.append(preprocess.pixel_size(n))
+    _, ny0, nx0 = data[0].shape
+    _, ny1, nx1 = data[C0].shape
+    p = pixel_ratio(sizes, C0, pixelratio)
+    refnew = [(nx0 - 1) / 2.0, (ny0 - 1) / 2.0]
+    refold = [(nx1 - 1) / 2.0, (ny1 - 1) / 2.0]
+    section0 = list(range(levels[0], levels[1] + 1, levels[2]))
+    if min(section0) < 0 or max(section0) >= ny0:
+        raise IndexError(f"Slice levels are not in a suitable scope. Must lie between 0 and Ny={ny0 - 1}. "
+                         "Aborting operation!")
+    z_, zu = coarse_section(min(section0), max(section0), p, refnew[1], refold[1], ny1, "cover")
+    section1 = list(range(z_, zu + 1))
+    print("Computing the Sinogram_levels:", section0)
+    print("Corresponds in the Lowresolution Sinograms to ", section1)
+    if zu < 1 or z_ > ny1:
+        eprint("!!!!!!!!!!! Warning: Section in lowresolution can not cover corresponding Section in High-resolution "
+               "data!!!!!!")
+    ratio = []
+    for i in range(C):  # ratio before the percentile scaling (:636-643)
+        sec = section1 if i >= C0 else section0
+        d = data[i]
+        ratio.append(np.sum(d[:, sec] / len(angles[i])))
+        d = d - np.percentile(d, scalepars[0])
+        data[i] = d / np.percentile(d, scalepars[1])
+    coll = []
+    for i in range(C):  # baseline per resolution (:646-664), then the slice selection (:666-669)
+        r = int(i >= C0)
+        s = _baseline(data[i], baseline[r], float(threshold[r]), noise[i], True)
+        coll.append(s[:, section1 if r else section0, :])
+    nd, nang0 = coll[0].shape[2], coll[0].shape[0]
+    nang1, nd1 = coll[C0].shape[0], coll[C0].shape[2]
+    possible = len(section0) if chunksize < 1 else min(len(section0), chunksize)
+    U = np.zeros([C, nx0, nx0, len(section0)])
+    new_sino = np.zeros([C0, nang0, len(section0), nd], np.float32)
+    new_sino_small = np.zeros([C1, nang1, len(section1), nd1], np.float32)
+    new_sino_high = np.zeros([C1, nang1, len(section0), nd], np.float32)
+    remaining = section0[:]
+    t0 = time.time()
+    while remaining:
+        if overlay > possible / 4.0:
+            overlay = int(possible / 4)
+            eprint(f"Overlap is too large for possible split size, reducing overlap to {overlay} which is a fourth "
+                   "of the possible splits.")
+        current = remaining[:min(possible, len(remaining))]
+        sp, ep = section0.index(current[0]), section0.index(current[-1])
+        cz_, czu = coarse_section(min(current), max(current), p, refnew[1], refold[1], ny1, "round")
+        sec1 = list(range(cz_, czu + 1))
+        a = possible - 2 * overlay if possible < len(remaining) else len(remaining)
+        ov_s = 0 if len(remaining) == len(section0) else overlay
+        ov_e = len(current) - len(remaining) if possible >= len(remaining) else overlay
+        sps, eps = section1.index(sec1[0]), section1.index(sec1[-1])
+        cur = [coll[i][:, sp:ep + 1, :] for i in range(C0)] + [coll[i][:, sps:eps + 1, :] for i in range(C0, C)]
+        topology = [C0, p, [refold[0], refold[1] - cz_], [refnew[0], refnew[1] - min(current)]]
+        info = [sp / float(len(section0)), len(current) / float(len(section0)), current]
+        try:
+            u_loc, s_loc = Reconstructionapproach3dsubsmapling(cur, angles, topology, (alpha[0], alpha[1]), mu,
+                                                               maxiter, device, [0, 0.1], levels[2], discrepancy,
+                                                               method, regularisation, info)
+        except GraptorMemoryError:
+            possible = int(possible * 0.7)
+            eprint(f"Warning: Computation requires too much memory, the problem is split, trying to compute "
+                   f"{possible} slices at once.")
+            if possible < 1:
+                raise MemoryError("Even a single slice requires too much memory.")
+            continue
+        except GraptorError as err:
+            possible = int(possible * 0.7)
+            eprint(f"An exception of type {type(err).__name__} occurred. Arguments:\n{err.args!r}")
+            if possible < 1:
+                raise
+            continue
+        remaining = remaining[a:]
+        U[:, :, :, sp + ov_s:ep + 1 - ov_e] = u_loc[:, :, :, ov_s:len(current) - ov_e]
+        new_sino[:, :, sp + ov_s:ep + 1 - ov_e, :] = s_loc[0][:, :, ov_s:len(current) - ov_e, :]
+        new_sino_high[:, :, sp + ov_s:ep + 1 - ov_e, :] = s_loc[1][:, :, ov_s:len(current) - ov_e, :]
+        new_sino_small[:, :, sps:eps + 1, :] = s_loc[2]
+    nz = len(section0)
+    sol = np.zeros([C, nz, nx0, nx0], np.float32)
+    for i in range(nz):
+        sol[:, i] = U[:, :, :, i]
+    ns, nsh, nss = new_sino.copy(), new_sino_high.copy(), new_sino_small.copy()
+    for i in range(C0):
+        fak = np.sum(ns[i]) / ratio[i]
+        sol[i] /= fak / len(angles[i])
+        ns[i] /= fak / len(angles[i])
+    for i in range(C1):
+        fak = np.sum(nss[i]) / ratio[i + C0]
+        sol[i + C0] /= fak / len(angles[i + C0])
+        nss[i] /= fak / len(angles[i + C0])
+        nsh /= fak / len(angles[i + C0])
+    for i in range(C):
+        mrc.write_mrc(f"{result}_{channelnames[i]}.mrc", sol[i])
+    for i in range(C1):
+        mrc.write_mrc(f"{result}_{channelnames[i + C0]}_sinogram_smallresu.mrc", nss[i])
+        mrc.write_mrc(f"{result}_{channelnames[i + C0]}_sinogram.mrc", nsh[i])
+    for i in range(C0):
+        mrc.write_mrc(f"{result}_{channelnames[i]}_sinogram.mrc", ns[i])
+    coll_u = np.zeros([nz, nx0, C * nx0], np.float32)
+    coll_n = np.zeros([nz, nx0, C * nx0], np.float32)
+    for j in range(C):
+        coll_u[:, :, j * nx0:(j + 1) * nx0] = np.transpose(U[j], (2, 0, 1))
+        coll_n[:, :, j * nx0:(j + 1) * nx0] = sol[j] / np.max(sol[j])
+    mrc.write_mrc(f"{result}_all_channels.mrc", coll_u)
+    mrc.write_mrc(f"{result}_all_channels_normalized.mrc", coll_n)
+    print("\nTime required for reconstruction:", int(10.0 * (time.time() - t0)) / 10.0, " seconds.\n")
+    return U
+
+
 def build_parser():
     p = argparse.ArgumentParser(prog="python -m graptor_gb300.cli",
                                 description="Multi-channel TV/TGV tomographic reconstruction (CUDA), with the options "
@@ -296,9 +472,10 @@ def main(argv=None):
     if setting == 2 and not args.Infiles_Smallresolution:
         eprint("Warning !!!! Only one type of data is given, changing method to 'Frobenius 3D Reconstruction'.")
         method, setting = "Frobenius 3D Reconstruction", 1
-    if setting == 2:
-        raise NotImplementedError("two-resolution subsampling (FrobSubs / UncorrSubs) is not built in graptor_gb300")
     names = resolve_names(list(args.Infiles))
+    C0 = len(names)
+    if setting == 2:  # the coarse channels follow the fine ones (:1005-1009)
+        names = names + resolve_names(list(args.Infiles_Smallresolution))
     disc = args.Discrepancy.upper()
     if disc not in ("KL", "L2"):
         eprint("Warning!!!!!! Discrepancy input not understood, set to KL (Kullback-Leibler). Possible choices are "
@@ -307,6 +484,8 @@ def main(argv=None):
     dh = list(args.Datahandling)
     defaults = ["bright", "thresholding", "0.000001", "", "0.05"]
     dh = (dh + defaults[len(dh):])[:5]
+    dh2 = list(args.Datahandling2)
+    dh2 = (dh2 + dh[len(dh2):])[:5]
     mu = list(np.ones(len(names)))
     for i in range(min(len(args.mu), len(names))):
         mu[i] = args.mu[i]
@@ -325,7 +504,14 @@ def main(argv=None):
     cfg = f"{args.Outfile}{method}_{mu}{alpha}_{args.Maxiter}Layer{levels}"
     with open(cfg + ".config", "w") as fh:
         fh.write(" " + str(args) + "\n")
-    if setting == 1:
+    pr = list(args.Pixelratio)
+    pr = pr[0] if len(pr) == 1 else pr[0] / pr[1]
+    if setting == 2:
+        handling = [[dh[k], dh2[k]] for k in range(5)]
+        u = reconstruct_subs(names, C0, args.Outfile, mu, alpha, args.Maxiter, method, levels, handling,
+                             [list(args.Badprojections), list(args.Badprojections2)], find_bad, chn, reg, disc, pr,
+                             args.Overlapping, args.Chunksize, args.Scalepars, device)
+    elif setting == 1:
         u = reconstruct_3d(names, args.Outfile, mu, alpha, args.Maxiter, method, levels, dh, args.Badprojections,
                            find_bad, chn, reg, disc, args.Overlapping, args.Chunksize, args.Scalepars, device)
     else:

@@ -78,6 +78,20 @@ def brightness_correction2(sino: np.ndarray) -> np.ndarray:
     return sino * (W / means)[:, None]
 
 
+def pixel_size(name: str) -> float:
+    """Detector pixel size recorded with a projection stack (``readh5alternative``,
+    h5utilities.py:421-475): ``Info/Dimensions/2`` second entry in HDF5 files,
+    -1 (unknown) for MRC stacks and when h5py is missing."""
+    if ".h5" not in name:
+        return -1.0
+    try:
+        import h5py
+    except ImportError:
+        return -1.0
+    with h5py.File(name, "r") as hf:
+        return float(np.array(hf.get("Info").get("Dimensions").get("2"))[1])
+
+
 def load_channel(name: str, brightness: str, badname: str, cutedges: float, bad_projections):
     """The loader the CLI picks by the brightness option (Reconstruction_coupled.py:148-155)."""
     if brightness.upper() == "BRIGHT":

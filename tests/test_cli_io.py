@@ -121,3 +121,23 @@ def test_bad_projections_match_reference(golden):
         for frac in ("0.15", "3"):
             got = badproj.find_bad_projections("stack", 4, float(frac) if "." in frac else int(frac), data=data)
             assert list(got) == list(g[f"{n}/bad_{frac}"]), (n, frac)
+
+
+def test_subsampling_geometry_helpers():
+    # sizes from the data win; a matching --Pixelratio is accepted, a different one aborts
+    assert cli.pixel_ratio([1.0, 1.0, 2.5], 2, -1) == 2.5
+    assert cli.pixel_ratio([1.0, 2.5], 1, 2.5004) == 2.5
+    with pytest.raises(ValueError):
+        cli.pixel_ratio([1.0, 2.5], 1, 3.0)
+    with pytest.raises(ValueError):
+        cli.pixel_ratio([1.0, 2.0, 2.5], 2, -1)
+    # MRC data carries no size: the input decides, and no input aborts
+    assert cli.pixel_ratio([-1.0, -1.0], 1, 2.0) == 2.0
+    with pytest.raises(ValueError):
+        cli.pixel_ratio([-1.0, -1.0], 1, -1)
+    # whole section covers with floor/ceil, a chunk rounds; both clip to the coarse stack
+    assert cli.coarse_section(2, 9, 2.0, 5.5, 2.5, 6, "cover") == (0, 5)
+    assert cli.coarse_section(2, 3, 2.0, 5.5, 2.5, 6, "cover") == (0, 2)
+    assert cli.coarse_section(2, 3, 2.0, 5.5, 2.5, 6, "round") == (1, 1)
+    assert cli.coarse_section(0, 40, 2.0, 5.5, 2.5, 6, "cover") == (0, 5)
+    assert preprocess.pixel_size("x.mrc") == -1.0
