@@ -228,10 +228,10 @@ std::map<TuneKey, std::tuple<int, int, int>> g_tune;
 
 int autotune(gt_problem *p) {
   const bool tgv = p->reg == GT_TGV;
-  // dual shape 2 (registers capped) measured faster alone but made the overlapped
-  // iteration slower (256^2 x 60 x 4: 1.251 against 1.223 ms); it is not tuned
+  // every dual shape is tuned: at 256^2 x 60 x 4 the order of the shapes timed
+  // alone is their order inside the overlapped iteration
   const int nc[3] = {gt::num_proj_configs(p->d.S, 0), gt::num_proj_configs(p->d.S, 1),
-                     std::min(2, gt::num_dual_configs(p->P))};
+                     gt::num_dual_configs(p->P)};
   p->P.fwd_cfg = 0;
   p->P.bp_cfg = 0;
   p->P.dual_cfg = 0;

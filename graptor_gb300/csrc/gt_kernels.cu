@@ -217,68 +217,12 @@ __device__ __forceinline__ float wnorm2(const float *w) {
   }
 }
 
-// ===========================================================================
-// k_dual: update_v (3-D :615-634, 2-D :265-284), update_w (3-D :637-660,
-// 2-D :286-304), NormV / NormW (3-D :290-610, 2-D :98-258)
-// thread = one (pixel, z); it owns all C channels of that voxel.
-// ===========================================================================
-template <int DIM, bool TGV, int CPL, int CMAX, int MINB = 1>
-__global__ void __launch_bounds__(256, MINB) k_dual(const IterParams P) {
+// projections of the dual variables onto the norm balls (NormV / NormW of the
+// coupling): vv, ww of the nC channels of one voxel, in place.
+template <int DIM, bool TGV, int CPL, int CMAX>
+__device__ __forceinline__ void dual_project(const IterParams &P, const int nC, float (&vv)[CMAX][DIM],
+                                             float (&ww)[CMAX][DIM == 3 ? 6 : 3]) {
   constexpr int K = DIM, KW = DIM == 3 ? 6 : 3;
-  const Dims d = P.d;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)d.N * d.N * d.Nz) return;
-  const int pix = (int)(t / d.Nz);
-  const int z = (int)(t - (long long)pix * d.Nz);
-  const int y = pix / d.N, x = pix - y * d.N;
-  const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
-  const float sigma = P.sigma;
-  const float *__restrict__ ub = P.ubar;
-  const float *__restrict__ pb = P.pbar;
-  const int nC = min(CMAX, d.C - P.cbase);  // channels of this launch (channel groups for uncorrelated C > 8)
-
-  float vv[CMAX][K], ww[CMAX][KW];
-#pragma unroll
-  for (int c = 0; c < CMAX; ++c) {
-    if (c >= nC) break;
-    const size_t i = (size_t)pix * S + (size_t)(P.cbase + c) * d.Nz + z;
-    // gradient of ubar: forward differences, zero at the last index
-    const float mu = -ub[i];
-    float g[3];
-    g[0] = (x < d.N - 1) ? mu + ub[i + S] : 0.f;
-    g[1] = (y < d.N - 1) ? mu + ub[i + rowS] : 0.f;
-    if (DIM == 3) g[2] = ((z < d.Nz - 1) ? mu + ub[i + 1] : 0.f) / P.stepsize;
-    float pc[3];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      pc[k] = TGV ? pb[k * vol + i] : 0.f;
-      vv[c][k] = P.v[k * vol + i] + sigma * (g[k] - pc[k]);
-    }
-    if (TGV) {
-      // symmetrised gradient of pbar: backward differences, zero at index 0
-      float a[3], b[3], cz[3];
-#pragma unroll
-      for (int k = 0; k < K; ++k) {
-        a[k] = x > 0 ? pc[k] - pb[k * vol + i - S] : 0.f;
-        b[k] = y > 0 ? pc[k] - pb[k * vol + i - rowS] : 0.f;
-        if (DIM == 3) cz[k] = (z > 0 ? pc[k] - pb[k * vol + i - 1] : 0.f) / P.stepsize;
-      }
-      float e[6];
-      if (DIM == 3) {
-        e[0] = a[0]; e[1] = b[1]; e[2] = cz[2];
-        e[3] = 0.5f * (a[1] + b[0]);
-        e[4] = 0.5f * (a[2] + cz[0]);
-        e[5] = 0.5f * (b[2] + cz[1]);
-      } else {
-        e[0] = a[0]; e[1] = b[1];
-        e[2] = 0.5f * (a[1] + b[0]);
-      }
-#pragma unroll
-      for (int k = 0; k < KW; ++k) ww[c][k] = P.w[k * vol + i] + sigma * e[k];
-    }
-  }
-
-  // ---- projections
   if (CPL == UNCORR) {
 #pragma unroll
     for (int c = 0; c < CMAX; ++c) {
@@ -374,11 +318,182 @@ __global__ void __launch_bounds__(256, MINB) k_dual(const IterParams P) {
     }
   }
 
+}
+
+// ===========================================================================
+// k_dual: update_v (3-D :615-634, 2-D :265-284), update_w (3-D :637-660,
+// 2-D :286-304), NormV / NormW (3-D :290-610, 2-D :98-258)
+// thread = one (pixel, z); it owns all C channels of that voxel.
+// ===========================================================================
+template <int DIM, bool TGV, int CPL, int CMAX, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) k_dual(const IterParams P) {
+  constexpr int K = DIM, KW = DIM == 3 ? 6 : 3;
+  const Dims d = P.d;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)d.N * d.N * d.Nz) return;
+  const int pix = (int)(t / d.Nz);
+  const int z = (int)(t - (long long)pix * d.Nz);
+  const int y = pix / d.N, x = pix - y * d.N;
+  const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
+  const float sigma = P.sigma;
+  const float *__restrict__ ub = P.ubar;
+  const float *__restrict__ pb = P.pbar;
+  const int nC = min(CMAX, d.C - P.cbase);  // channels of this launch (channel groups for uncorrelated C > 8)
+
+  float vv[CMAX][K], ww[CMAX][KW];
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c) {
+    if (c >= nC) break;
+    const size_t i = (size_t)pix * S + (size_t)(P.cbase + c) * d.Nz + z;
+    // gradient of ubar: forward differences, zero at the last index
+    const float mu = -ub[i];
+    float g[3];
+    g[0] = (x < d.N - 1) ? mu + ub[i + S] : 0.f;
+    g[1] = (y < d.N - 1) ? mu + ub[i + rowS] : 0.f;
+    if (DIM == 3) g[2] = ((z < d.Nz - 1) ? mu + ub[i + 1] : 0.f) / P.stepsize;
+    float pc[3];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      pc[k] = TGV ? pb[k * vol + i] : 0.f;
+      vv[c][k] = P.v[k * vol + i] + sigma * (g[k] - pc[k]);
+    }
+    if (TGV) {
+      // symmetrised gradient of pbar: backward differences, zero at index 0
+      float a[3], b[3], cz[3];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        a[k] = x > 0 ? pc[k] - pb[k * vol + i - S] : 0.f;
+        b[k] = y > 0 ? pc[k] - pb[k * vol + i - rowS] : 0.f;
+        if (DIM == 3) cz[k] = (z > 0 ? pc[k] - pb[k * vol + i - 1] : 0.f) / P.stepsize;
+      }
+      float e[6];
+      if (DIM == 3) {
+        e[0] = a[0]; e[1] = b[1]; e[2] = cz[2];
+        e[3] = 0.5f * (a[1] + b[0]);
+        e[4] = 0.5f * (a[2] + cz[0]);
+        e[5] = 0.5f * (b[2] + cz[1]);
+      } else {
+        e[0] = a[0]; e[1] = b[1];
+        e[2] = 0.5f * (a[1] + b[0]);
+      }
+#pragma unroll
+      for (int k = 0; k < KW; ++k) ww[c][k] = P.w[k * vol + i] + sigma * e[k];
+    }
+  }
+
+  dual_project<DIM, TGV, CPL, CMAX>(P, nC, vv, ww);
+
   // ---- store
 #pragma unroll
   for (int c = 0; c < CMAX; ++c) {
     if (c >= nC) break;
     const size_t i = (size_t)pix * S + (size_t)(P.cbase + c) * d.Nz + z;
+#pragma unroll
+    for (int k = 0; k < K; ++k) P.v[k * vol + i] = vv[c][k];
+    if (TGV) {
+#pragma unroll
+      for (int k = 0; k < KW; ++k) P.w[k * vol + i] = ww[c][k];
+    }
+  }
+}
+
+// k_dual_pf: k_dual for a launch whose channel count is exactly CN (no channel
+// guard), the operands of a channel -- ubar at the voxel and its three forward
+// neighbours, pbar at the voxel and its three backward neighbours, v and w --
+// loaded LA channels ahead of their arithmetic (LA = CN: every load before any
+// arithmetic).  k_dual interleaves each channel's loads with its arithmetic and
+// keeps few loads in flight (it is DRAM-latency bound); here a thread has up to
+// 25 LA loads in flight.  The arithmetic is k_dual's, operation by operation, so
+// the iterates are bit-identical.
+template <int DIM, bool TGV, int CPL, int CN, int MINB = 1, int NT = 256, int LA = CN>
+__global__ void __launch_bounds__(NT, MINB) k_dual_pf(const IterParams P) {
+  constexpr int K = DIM, KW = DIM == 3 ? 6 : 3;
+  const Dims d = P.d;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)d.N * d.N * d.Nz) return;
+  const int pix = (int)(t / d.Nz);
+  const int z = (int)(t - (long long)pix * d.Nz);
+  const int y = pix / d.N, x = pix - y * d.N;
+  const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
+  const bool hx = x < d.N - 1, hy = y < d.N - 1, hz = z < d.Nz - 1;  // forward neighbours exist
+  const bool lx = x > 0, ly = y > 0, lz = z > 0;                      // backward neighbours exist
+  const float *__restrict__ ub = P.ubar;
+  const float *__restrict__ pb = P.pbar;
+  const size_t i0 = (size_t)pix * S + (size_t)P.cbase * d.Nz + z;
+  const float sigma = P.sigma;
+
+  float u0[CN], ux[CN], uy[CN], uz[CN];
+  float p0[CN][K], px[CN][K], py[CN][K], pz[CN][K];
+  float vo[CN][K], wo[CN][KW];
+  float vv[CN][K], ww[CN][KW];
+  auto load = [&](const int c) {
+    const size_t i = i0 + (size_t)c * d.Nz;
+    u0[c] = ub[i];
+    ux[c] = hx ? ub[i + S] : 0.f;
+    uy[c] = hy ? ub[i + rowS] : 0.f;
+    if (DIM == 3) uz[c] = hz ? ub[i + 1] : 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      vo[c][k] = P.v[k * vol + i];
+      if (TGV) {
+        p0[c][k] = pb[k * vol + i];
+        px[c][k] = lx ? pb[k * vol + i - S] : 0.f;
+        py[c][k] = ly ? pb[k * vol + i - rowS] : 0.f;
+        if (DIM == 3) pz[c][k] = lz ? pb[k * vol + i - 1] : 0.f;
+      }
+    }
+    if (TGV) {
+#pragma unroll
+      for (int k = 0; k < KW; ++k) wo[c][k] = P.w[k * vol + i];
+    }
+  };
+  auto compute = [&](const int c) {
+    const float mu = -u0[c];
+    float g[3];
+    g[0] = hx ? mu + ux[c] : 0.f;
+    g[1] = hy ? mu + uy[c] : 0.f;
+    if (DIM == 3) g[2] = (hz ? mu + uz[c] : 0.f) / P.stepsize;
+    float pc[3];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      pc[k] = TGV ? p0[c][k] : 0.f;
+      vv[c][k] = vo[c][k] + sigma * (g[k] - pc[k]);
+    }
+    if (TGV) {
+      float a[3], b[3], cz[3];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        a[k] = lx ? pc[k] - px[c][k] : 0.f;
+        b[k] = ly ? pc[k] - py[c][k] : 0.f;
+        if (DIM == 3) cz[k] = (lz ? pc[k] - pz[c][k] : 0.f) / P.stepsize;
+      }
+      float e[6];
+      if (DIM == 3) {
+        e[0] = a[0]; e[1] = b[1]; e[2] = cz[2];
+        e[3] = 0.5f * (a[1] + b[0]);
+        e[4] = 0.5f * (a[2] + cz[0]);
+        e[5] = 0.5f * (b[2] + cz[1]);
+      } else {
+        e[0] = a[0]; e[1] = b[1];
+        e[2] = 0.5f * (a[1] + b[0]);
+      }
+#pragma unroll
+      for (int k = 0; k < KW; ++k) ww[c][k] = wo[c][k] + sigma * e[k];
+    }
+  };
+#pragma unroll
+  for (int c = 0; c < LA && c < CN; ++c) load(c);
+#pragma unroll
+  for (int c = 0; c < CN; ++c) {
+    if (c + LA < CN) load(c + LA);
+    compute(c);
+  }
+
+  dual_project<DIM, TGV, CPL, CN>(P, CN, vv, ww);
+
+#pragma unroll
+  for (int c = 0; c < CN; ++c) {
+    const size_t i = i0 + (size_t)c * d.Nz;
 #pragma unroll
     for (int k = 0; k < K; ++k) P.v[k * vol + i] = vv[c][k];
     if (TGV) {
@@ -1911,8 +2026,10 @@ bool dual_z2_ok(const IterParams &P, int tgv, int cpl) {
 }
 
 // dual launch shapes: 0 k_dual, 1 k_dual_z2 (where dual_z2_ok; else the same as 0),
-// 2 k_dual with registers capped for 5 resident blocks (C <= 4; else as 0)
-int num_dual_configs(const IterParams &P) { return P.d.C <= 4 ? 3 : 1; }
+// 2 k_dual with registers capped for 5 resident blocks (C <= 4; else as 0),
+// 3-5 k_dual_pf: loads one channel ahead in 128-thread blocks (3), all loads first
+// in 128-thread (4) or 64-thread (5) blocks (C <= 4; else as 0)
+int num_dual_configs(const IterParams &P) { return P.d.C <= 4 ? 6 : 1; }
 
 template <int CPL>
 static void launch_dual_z2(const IterParams &P, cudaStream_t st) {
@@ -1923,6 +2040,16 @@ static void launch_dual_z2(const IterParams &P, cudaStream_t st) {
   else k_dual_z2<CPL, 4><<<g, 256, 0, st>>>(P);
 }
 
+template <int DIM, bool TGV, int CPL, int MINB, int NT, int LA = 4>
+static void launch_dual_pf(const IterParams &P, cudaStream_t st) {
+  const unsigned g = blocks_for((long long)P.d.N * P.d.N * P.d.Nz, NT);
+  const int C = P.d.C;
+  if (C == 1) k_dual_pf<DIM, TGV, CPL, 1, MINB, NT, 1><<<g, NT, 0, st>>>(P);
+  else if (C == 2) k_dual_pf<DIM, TGV, CPL, 2, MINB, NT, LA < 2 ? LA : 2><<<g, NT, 0, st>>>(P);
+  else if (C == 3) k_dual_pf<DIM, TGV, CPL, 3, MINB, NT, LA < 3 ? LA : 3><<<g, NT, 0, st>>>(P);
+  else k_dual_pf<DIM, TGV, CPL, 4, MINB, NT, LA><<<g, NT, 0, st>>>(P);
+}
+
 template <int DIM, bool TGV, int CPL>
 static cudaError_t launch_dual_c(const IterParams &P, cudaStream_t st) {
   const long long n = (long long)P.d.N * P.d.N * P.d.Nz;
@@ -1930,6 +2057,12 @@ static cudaError_t launch_dual_c(const IterParams &P, cudaStream_t st) {
   const int C = P.d.C;
   if (DIM == 3 && TGV && CPL != NUCL && P.dual_cfg == 1 && C <= 4 && P.d.Nz % 2 == 0) {
     launch_dual_z2<CPL == NUCL ? FROB : CPL>(P, st);
+    return cudaGetLastError();
+  }
+  if (P.dual_cfg >= 3 && C <= 4) {  // operands loaded ahead of the arithmetic
+    if (P.dual_cfg == 3) launch_dual_pf<DIM, TGV, CPL, 5, 128, 1>(P, st);  // one channel ahead, 96 registers
+    else if (P.dual_cfg == 4) launch_dual_pf<DIM, TGV, CPL, 4, 128>(P, st);  // all channels, 128 registers
+    else launch_dual_pf<DIM, TGV, CPL, 8, 64>(P, st);                        // as 4 in 64-thread blocks
     return cudaGetLastError();
   }
   if (P.dual_cfg == 2 && C <= 4) {  // registers capped for 5 resident blocks

@@ -241,10 +241,13 @@ def test_projector_launch_shapes_give_identical_iterates(S_case):
                 np.testing.assert_array_equal(got[k], ref[k], err_msg=f"fwd {fc} bp {bc} field {k}")
 
 
-@pytest.mark.parametrize("C,cpl", [(1, "FROB"), (2, "FROB"), (3, "UNCORR"), (4, "FROB")])
-def test_dual_launch_shapes_give_identical_iterates(C, cpl):
-    """The two-slice float2 dual kernel and the register-capped one compute every
-    value with the same operations as the one-slice kernel: identical iterates."""
+@pytest.mark.parametrize("dim,C,cpl,reg", [(3, 1, "FROB", "TGV"), (3, 2, "FROB", "TGV"), (3, 3, "UNCORR", "TGV"),
+                                           (3, 4, "FROB", "TGV"), (3, 3, "FROB", "TGV"), (3, 2, "NUCL", "TGV"),
+                                           (3, 4, "FROB", "TV"), (2, 4, "FROB", "TGV"), (2, 2, "NUCL", "TGV")])
+def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg):
+    """The two-slice float2 dual kernel, the register-capped one and the kernels that
+    load every operand before the arithmetic compute every value with the same
+    operations as the one-slice kernel: identical iterates."""
     from graptor_gb300 import phantom
     from graptor_gb300.solver import Problem
     N, Nz, nang = 28, 6, 15
@@ -252,18 +255,25 @@ def test_dual_launch_shapes_give_identical_iterates(C, cpl):
     ang = phantom.angles_deg(nang)
     f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
     got = []
-    with Problem(3, N, Nz, C, N, ang, (4, 1), [0.3] * C, coupling=cpl, normest=17.0, stepsize=2.0) as p:
-        for shape in (0, 1, 2):
+    z2 = dim == 3 and reg == "TGV" and cpl != "NUCL"
+    shapes = (0, 1, 2, 3, 4, 5) if z2 else (0, 2, 3, 4, 5)
+    fields = ("u", "v", "w", "p") if reg == "TGV" else ("u", "v")
+    with Problem(dim, N, Nz, C, N, ang, (4, 1), [0.3] * C, regularisation=reg, coupling=cpl, normest=17.0,
+                 stepsize=2.0) as p:
+        for shape in shapes:
             p.set_data(f)
             p.set_dual_shape(shape)
             p.run(9).synchronize()
-            got.append({k: p.get(k) for k in ("u", "v", "w", "p")})
+            got.append({k: p.get(k) for k in fields})
         with pytest.raises(ValueError):
-            p.set_dual_shape(3)
+            p.set_dual_shape(6)
+        if not z2:
+            with pytest.raises(ValueError):
+                p.set_dual_shape(1)
     for g in got[1:]:
         for k in got[0]:
             np.testing.assert_array_equal(g[k], got[0][k], err_msg=k)
-    with Problem(3, N, 5, C, N, ang, (4, 1), [0.3] * C, normest=17.0) as q:  # odd Nz: one shape only
+    with Problem(3, N, 5, C, N, ang, (4, 1), [0.3] * C, normest=17.0) as q:  # odd Nz: no two-slice shape
         with pytest.raises(ValueError):
             q.set_dual_shape(1)
 
