@@ -1,6 +1,7 @@
 // C ABI of the GB300 primal-dual TGV/TV reconstruction (declared in
 // include/graptor_gb300.h): problem handles, host<->device layout changes,
 // step-size setup and the graph-captured iteration loop.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -21,6 +22,7 @@
 
 namespace gt {
 cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st);
+cudaError_t prepare_bp_tma();
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st);
 cudaError_t launch_bp(const IterParams &P, cudaStream_t st);
 cudaError_t launch_update(const IterParams &P, int tgv, cudaStream_t st);
@@ -112,6 +114,41 @@ void angle_table(const double *angles, int N, int nd, int nang, std::vector<doub
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// cuTensorMapEncodeTiled from the driver (through the runtime's entry-point query,
+// so the library needs no link against libcuda)
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void *ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(ptr);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// TMA descriptor of lambda [nang][nd][S] for k_bp_tma: boxes of 16 bins x
+// `slices` slices of one angle, zero fill outside.  False where S % 4 != 0 or the driver
+// declines; the back projection then keeps its other shapes.
+bool encode_lambda_map(CUtensorMap *map, float *lam, int S, int nd, int nang, unsigned slices) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || S % 4 != 0 || reinterpret_cast<uintptr_t>(lam) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)S, (cuuint64_t)nd, (cuuint64_t)nang};
+  const cuuint64_t strides[2] = {(cuuint64_t)S * sizeof(float), (cuuint64_t)nd * S * sizeof(float)};
+  const cuuint32_t box[3] = {slices, 16, 1};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, lam, dims, strides, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
 struct gt_problem {
@@ -144,6 +181,9 @@ struct gt_problem {
   long long iters = 0;
   bool has_data = false;
   double lsqr = 0;             // > 0: step-size constant of a variant (two-resolution solver: 36)
+  int *flags = nullptr;        // device error flags (P.err)
+  CUtensorMap bp_tmap{};       // TMA descriptors of lambda for k_bp_tma, boxes of 128 and 256
+  CUtensorMap bp_tmap_wide{};  // slices (valid when P.bp_tmap / P.bp_tmap_wide are set)
 };
 
 namespace {
@@ -230,7 +270,10 @@ int autotune(gt_problem *p) {
   const bool tgv = p->reg == GT_TGV;
   // every dual shape is tuned: at 256^2 x 60 x 4 the order of the shapes timed
   // alone is their order inside the overlapped iteration
-  const int nc[3] = {gt::num_proj_configs(p->d.S, 0), gt::num_proj_configs(p->d.S, 1),
+  // back-projection shapes 14 and 15 (TMA-staged sinogram rows) are bit-identical
+  // but slower on every measured workload (256^2 x 60 x 4: 0.43 / 0.45 against
+  // 0.36 ms); they stay selectable by gt_set_tuning and are not tuned
+  const int nc[3] = {gt::num_proj_configs(p->d.S, 0), std::min(14, gt::num_proj_configs(p->d.S, 1)),
                      gt::num_dual_configs(p->P)};
   p->P.fwd_cfg = 0;
   p->P.bp_cfg = 0;
@@ -388,7 +431,8 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
       align256(fb), align256(fb), align256(fb),                     // lam, f, ku
       align256(std::max(fv, fb)),                                   // stage
       align256(fv),                                                 // kstar
-      align256(sizeof(double) * D.C)};                              // mu (double)
+      align256(sizeof(double) * D.C),                               // mu (double)
+      align256(sizeof(int) * 4)};                                   // error flags
   const int nsz = (int)(sizeof(sizes) / sizeof(sizes[0]));
   for (int k = 0; k < nsz; ++k) { off[k] = total; total += sizes[k]; }
   cudaError_t e = cudaMalloc(&p->block, total);
@@ -413,6 +457,7 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
   p->stage = (float *)(b + off[12]);
   p->kstar = (float *)(b + off[13]);
   p->mu64 = (double *)(b + off[14]);
+  p->flags = (int *)(b + off[15]);
 
   std::vector<float> t32((size_t)D.nang * 4);
   for (size_t k = 0; k < t32.size(); ++k) t32[k] = (float)p->ofs64h[k];
@@ -493,6 +538,14 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
   P.ofs = p->ofs; P.mu = p->mu_eff;
   P.u = p->u; P.ubar = p->ubar; P.p = p->p; P.pbar = p->pbar; P.v = p->v; P.w = p->w;
   P.lam = p->lam; P.f = p->f; P.ku = p->ku; P.kstar = p->kstar; P.mu64 = p->mu64;
+  P.err = p->flags;
+  P.bp_tmap = encode_lambda_map(&p->bp_tmap, p->lam, p->d.S, p->d.nd, p->d.nang, 128) ? &p->bp_tmap : nullptr;
+  P.bp_tmap_wide =
+      encode_lambda_map(&p->bp_tmap_wide, p->lam, p->d.S, p->d.nd, p->d.nang, 256) ? &p->bp_tmap_wide : nullptr;
+  if (P.bp_tmap_wide && gt::prepare_bp_tma() != cudaSuccess) {
+    cudaGetLastError();
+    P.bp_tmap_wide = nullptr;
+  }
   *out = p;
   return GT_OK;
 }
@@ -599,6 +652,12 @@ int gt_synchronize(gt_problem *p) {
   if (!p) return set_err(GT_ERR_ARG, "null problem");
   CK(cudaSetDevice(p->device));
   CK(cudaStreamSynchronize(p->stream));
+  int flag = 0;
+  CK(cudaMemcpy(&flag, p->flags, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag) {
+    CK(cudaMemset(p->flags, 0, sizeof(int)));
+    return set_err(GT_ERR_TIMEOUT, "a back-projection block gave up waiting for its TMA copies; the iterate is invalid");
+  }
   return GT_OK;
 }
 

@@ -57,6 +57,9 @@ struct IterParams {
   float *kstar;          // [vol] back projection K* lambda
   const double *mu64;    // [C] mu (KL) or mu (L2) in double, for the gap
   double ne64;           // operator-norm estimate, for the gap
+  const void *bp_tmap;   // host copies of the TMA descriptors of lambda for k_bp_tma with
+  const void *bp_tmap_wide;  // 128- and 256-slice boxes, or null
+  int *err;              // device flag: a kernel gave up a bounded wait (read by gt_synchronize)
 };
 
 }  // namespace gt

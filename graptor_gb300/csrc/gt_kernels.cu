@@ -21,6 +21,7 @@
 #include <math.h>
 
 #include "gt_common.cuh"
+#include "gt_tma.cuh"
 
 namespace gt {
 
@@ -1461,6 +1462,167 @@ __global__ void __launch_bounds__(256) k_bp(const IterParams P) {
   sl.store(P.kstar + (size_t)pix * d.S, acc);
 }
 
+// k_bp_tma: back projection with the sinogram rows a pixel tile needs staged in
+// shared memory by TMA.  A block owns an 8 x 8 pixel tile and 128 slices (one
+// float4 per lane); per angle the tile's taps fall on at most 13 consecutive
+// bins (the detector coordinate moves by |cos| + |sin| <= 1.4143 per pixel step),
+// so one 16-bin x 128-slice box of lambda is copied per angle into a 4-stage ring
+// while the previous angles are summed.  Warp w owns row y0 + w; lanes 0..7
+// compute the geometry of the row's 8 pixels and broadcast it by shuffles, so
+// the geometry is computed once per pixel and angle instead of once per slice
+// group.  Every pixel adds its taps in the reference's order (angles ascending,
+// lower tap then upper tap) with radon_ad's weights (3-D :832-839), as k_bp does,
+// so the iterates are bit-identical.  Every wait on a copy is bounded: a block
+// that gives up sets P.err, waits (bounded) for its copies in flight and leaves
+// without storing.
+constexpr int BPT_ST = 4, BPT_BINS = 16, BPT_TILE = 8;
+constexpr uint32_t BPT_WAIT_LIMIT = 1u << 22;
+
+// lowest bin the taps of the tile at (x0, y0) can touch for angle o: the floor of
+// the smallest detector coordinate of the tile's corners, minus one for the
+// rounding of interior pixels
+__device__ __forceinline__ int bp_tile_lo(const float4 o, int x0, int y0) {
+  float m = 3.0e38f;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float cx = (float)(x0 + (c & 1) * (BPT_TILE - 1)), cy = (float)(y0 + (c >> 1) * (BPT_TILE - 1));
+    m = fminf(m, __fadd_rn(__fadd_rn(__fmul_rn(cx, o.x), __fmul_rn(cy, o.y)), o.z));
+  }
+  return (int)floorf(m) - 1;
+}
+
+template <int VW>
+__device__ __forceinline__ void bpt_tap(float (&acc)[VW], float w, float4 a, float4 b) {
+  acc[0] = __fmaf_rn(w, a.x, acc[0]); acc[1] = __fmaf_rn(w, a.y, acc[1]);
+  acc[2] = __fmaf_rn(w, a.z, acc[2]); acc[3] = __fmaf_rn(w, a.w, acc[3]);
+  if (VW == 8) {
+    acc[4 % VW] = __fmaf_rn(w, b.x, acc[4 % VW]); acc[5 % VW] = __fmaf_rn(w, b.y, acc[5 % VW]);
+    acc[6 % VW] = __fmaf_rn(w, b.z, acc[6 % VW]); acc[7 % VW] = __fmaf_rn(w, b.w, acc[7 % VW]);
+  }
+}
+
+// VW = 4: a block covers 128 slices (one float4 per lane); VW = 8: 256 slices (two
+// float4 per lane, slices 4l.. and 128+4l.., as Slices<8>)
+template <int VW>
+__global__ void __launch_bounds__(256) k_bp_tma(const IterParams P, const __grid_constant__ CUtensorMap tm) {
+  constexpr int SC = 32 * VW;
+  extern __shared__ __align__(128) float stage[];  // [BPT_ST][BPT_BINS][SC]
+  __shared__ __align__(8) uint64_t full[BPT_ST];
+  const Dims d = P.d;
+  const int ntx = (d.N + BPT_TILE - 1) / BPT_TILE;
+  const int bid = blockIdx.x;
+  const int tx = bid % ntx, ty = (bid / ntx) % ntx, ch = bid / (ntx * ntx);
+  const int x0 = BPT_TILE * tx, y0 = BPT_TILE * ty, sb = ch * SC;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int y = y0 + warp;
+  const int sa = sb + 4 * lane, sbb = sa + 128;  // this lane's float4 chunks (the second for VW = 8)
+  const int nang = d.nang, nd = d.nd;
+  const float fnd = (float)nd;
+  constexpr uint32_t BOX = BPT_BINS * SC * sizeof(float);
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < BPT_ST; ++k) mbar_init(&full[k], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  auto issue = [&](int j) {
+    const int st = j % BPT_ST;
+    mbar_arrive_expect_tx(&full[st], BOX);
+    tma_load_3d(stage + (size_t)st * BPT_BINS * SC, &tm, &full[st], sb, bp_tile_lo(__ldg(P.ofs + j), x0, y0), j);
+  };
+  if (threadIdx.x == 0)
+    for (int j = 0; j < BPT_ST && j < nang; ++j) issue(j);
+
+  float acc[BPT_TILE][VW];
+#pragma unroll
+  for (int r = 0; r < BPT_TILE; ++r)
+#pragma unroll
+    for (int k = 0; k < VW; ++k) acc[r][k] = 0.f;
+  bool tmo = nang > 0 && !mbar_wait_bounded(&full[0], 0, BPT_WAIT_LIMIT);
+  int j = 0;
+  for (; j < nang; ++j) {
+    // every thread has waited for angle j's copy; all have finished angle j - 1
+    if (__syncthreads_or(tmo)) break;
+    if (threadIdx.x == 0 && j >= 1 && j - 1 + BPT_ST < nang) issue(j - 1 + BPT_ST);  // into the freed stage
+    const int st = j % BPT_ST;
+    const float4 o = __ldg(P.ofs + j);
+    const int lo = bp_tile_lo(o, x0, y0);
+    const int xr = x0 + (lane & (BPT_TILE - 1));
+    const float tt = __fadd_rn(__fadd_rn(__fmul_rn((float)xr, o.x), __fmul_rn((float)y, o.y)), o.z);
+    const bool in = xr < d.N && y < d.N && tt > -1.f && tt < fnd;
+    const float fl = floorf(tt);
+    const float pw = fminf(__fsub_rn(tt, fl), 0x1.fffffep-1f);
+    const int rel = in ? (int)fl - lo : INT_MIN;
+    const float *srow = stage + (size_t)st * BPT_BINS * SC + 4 * lane;
+#pragma unroll
+    for (int r = 0; r < BPT_TILE; ++r) {
+      const int rr = __shfl_sync(0xffffffffu, rel, r);
+      const float p = __shfl_sync(0xffffffffu, pw, r);
+      if (rr == INT_MIN) continue;  // pixel outside the image or the detector for this angle
+      const float q = __fsub_rn(1.0f, p);
+      const int il = rr + lo;
+      const bool tlo = il >= 0, thi = il <= nd - 2;
+      float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, b0 = a0, b1 = a0;
+      if (rr >= 0 && rr <= BPT_BINS - 2) {
+        const float *ra = srow + rr * SC;
+        if (tlo) {
+          a0 = *reinterpret_cast<const float4 *>(ra);
+          if (VW == 8) a1 = *reinterpret_cast<const float4 *>(ra + 128);
+        }
+        if (thi) {
+          b0 = *reinterpret_cast<const float4 *>(ra + SC);
+          if (VW == 8) b1 = *reinterpret_cast<const float4 *>(ra + SC + 128);
+        }
+      } else {  // outside the staged bins (not reached): read lambda directly
+        const float *lj = P.lam + (size_t)j * nd * d.S;
+        if (tlo && sa < d.S) a0 = *reinterpret_cast<const float4 *>(lj + (size_t)il * d.S + sa);
+        if (tlo && VW == 8 && sbb < d.S) a1 = *reinterpret_cast<const float4 *>(lj + (size_t)il * d.S + sbb);
+        if (thi && sa < d.S) b0 = *reinterpret_cast<const float4 *>(lj + (size_t)(il + 1) * d.S + sa);
+        if (thi && VW == 8 && sbb < d.S) b1 = *reinterpret_cast<const float4 *>(lj + (size_t)(il + 1) * d.S + sbb);
+      }
+      if (tlo) bpt_tap<VW>(acc[r], q, a0, a1);
+      if (thi) bpt_tap<VW>(acc[r], p, b0, b1);
+    }
+    if (j + 1 < nang) tmo = !mbar_wait_bounded(&full[(j + 1) % BPT_ST], ((j + 1) / BPT_ST) & 1, BPT_WAIT_LIMIT);
+  }
+  if (j < nang) {
+    // gave up waiting for angle j: flag it, let the copies in flight (angles j ..
+    // the last issued) land, leave without storing
+    if (threadIdx.x == 0) {
+      atomicExch(P.err, 1);
+      const int last = min(nang - 1, j >= 2 ? j - 2 + BPT_ST : BPT_ST - 1);
+      for (int a = j; a <= last; ++a) mbar_wait_bounded(&full[a % BPT_ST], (a / BPT_ST) & 1, BPT_WAIT_LIMIT);
+    }
+    return;
+  }
+  if (y < d.N) {
+#pragma unroll
+    for (int r = 0; r < BPT_TILE; ++r) {
+      if (x0 + r >= d.N) continue;
+      float *o = P.kstar + ((size_t)y * d.N + x0 + r) * d.S;
+      if (sa < d.S) *reinterpret_cast<float4 *>(o + sa) = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+      if (VW == 8 && sbb < d.S)
+        *reinterpret_cast<float4 *>(o + sbb) =
+            make_float4(acc[r][4 % VW], acc[r][5 % VW], acc[r][6 % VW], acc[r][7 % VW]);
+    }
+  }
+}
+
+template <int VW>
+static void bp_tma(const IterParams &P, cudaStream_t st) {
+  constexpr int SC = 32 * VW;
+  const int ntx = (P.d.N + BPT_TILE - 1) / BPT_TILE;
+  const unsigned g = (unsigned)ntx * ntx * ((P.d.S + SC - 1) / SC);
+  const size_t smem = (size_t)BPT_ST * BPT_BINS * SC * sizeof(float);
+  k_bp_tma<VW><<<g, 256, smem, st>>>(P, *static_cast<const CUtensorMap *>(VW == 8 ? P.bp_tmap_wide : P.bp_tmap));
+}
+
+// shared-memory limits of the TMA back projection (64 KB of stages for 256-slice
+// boxes), set once per problem on its device before any launch or capture
+cudaError_t prepare_bp_tma() {
+  return cudaFuncSetAttribute(k_bp_tma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)((size_t)BPT_ST * BPT_BINS * 256 * sizeof(float)));
+}
+
 // k_update: update_u + update_p + extrapolation for UW consecutive slices.
 template <int DIM, bool TGV, int UW>
 __global__ void __launch_bounds__(256) k_update(const IterParams P) {
@@ -2301,7 +2463,7 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // which keeps all lanes busy when S is small.
 int num_proj_configs(int S, int which) {
   if (S % 4 != 0) return 1;
-  return which == 0 ? 14 : 14;  // configs 4 / 8 (one slice per thread) stay candidates for every S
+  return which == 0 ? 14 : 16;  // configs 4 / 8 (one slice per thread) stay candidates for every S
 }
 
 template <int VW, int UNR>
@@ -2406,6 +2568,12 @@ cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
       case 11: bp_run<8, 8>(P, st); break;
       case 12: bp_run<4, 4>(P, st); break;
       case 13: bp_wl(P, st); break;
+      case 14:  // no descriptor: the one-angle shape (identical sums)
+        if (P.bp_tmap) bp_tma<4>(P, st); else bp_vw<8, 1, false>(P, st);
+        break;
+      case 15:
+        if (P.bp_tmap_wide) bp_tma<8>(P, st); else bp_vw<8, 1, false>(P, st);
+        break;
       default: bp_vw<8, 2>(P, st); break;
     }
   } else if (S % 2 == 0) {

@@ -209,7 +209,7 @@ def test_state_roundtrip_and_warm_start():
         assert p.scalars["normest"] == 15.0
 
 
-@pytest.mark.parametrize("S_case", [(40, 3, 2, 21), (36, 16, 1, 17)], ids=["S6", "S16"])
+@pytest.mark.parametrize("S_case", [(40, 3, 2, 21), (36, 16, 1, 17), (41, 4, 2, 19)], ids=["S6", "S16", "S8odd"])
 def test_projector_launch_shapes_give_identical_iterates(S_case):
     """Every forward / back projection launch shape the autotuner can pick sums the
     same terms in the same order, so the iterates agree bit for bit."""
@@ -225,7 +225,7 @@ def test_projector_launch_shapes_give_identical_iterates(S_case):
         from graptor_gb300 import _lib as L
         nf = L.lib().gt_set_tuning(p._h, 99, 0)
         assert nf != 0  # out of range is refused
-        configs = [(fc, 0) for fc in range(12)] + [(0, bc) for bc in range(1, 14)] if (C * Nz) % 4 == 0 else [(0, 0)]
+        configs = [(fc, 0) for fc in range(14)] + [(0, bc) for bc in range(1, 16)] if (C * Nz) % 4 == 0 else [(0, 0)]
         for fc, bc in configs:
             p.set_data(f)
             try:
