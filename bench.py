@@ -254,9 +254,13 @@ def run_ours(args, rank, world, local):
     Sb = N * nang * S
     f = np.concatenate([np.transpose(s, (1, 0, 2)) for s in sino])  # [S, nang, nd]
     stream = torch.cuda.Stream()
+    forced = args.fwd_shape is not None or args.bp_shape is not None or args.dual_shape is not None
     prob = Problem(3, N, Nz, C, N, ang, W["alpha"], W["mu"], "KL", "TGV", "FROB", 1.0, None, local,
-                   stream.cuda_stream)
+                   stream.cuda_stream, autotune=not forced)
     prob.set_data(f)
+    if forced:  # launch shapes given on the command line (profiler captures): no tuning launches
+        prob.set_tuning(args.fwd_shape or 0, args.bp_shape or 0)
+        prob.set_dual_shape(args.dual_shape or 0)
     prob.run(args.warmup).synchronize()
 
     # ---- device-timed region: K iterations, inputs resident in HBM
@@ -548,6 +552,10 @@ def main():
     ap.add_argument("--batch", type=int, default=64, help="problems per rank for --workload batched")
     ap.add_argument("--seeds", type=int, default=8, help="held-out problems per rank for --workload warmstart")
     ap.add_argument("--weights", default=None, help="network weights for --workload warmstart")
+    ap.add_argument("--fwd-shape", type=int, default=None,
+                    help="force the forward projector's launch shape (no autotuning); profiler captures")
+    ap.add_argument("--bp-shape", type=int, default=None, help="force the back projector's launch shape")
+    ap.add_argument("--dual-shape", type=int, default=None, help="force the dual kernel's launch shape")
     ap.add_argument("--quick", action="store_true",
                     help="only the device-timed region (no e2e, kernel timing or CPU baseline): profiler runs")
     args = ap.parse_args()
