@@ -539,6 +539,8 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
   P.u = p->u; P.ubar = p->ubar; P.p = p->p; P.pbar = p->pbar; P.v = p->v; P.w = p->w;
   P.lam = p->lam; P.f = p->f; P.ku = p->ku; P.kstar = p->kstar; P.mu64 = p->mu64;
   P.err = p->flags;
+  P.bp_skip_angle = -1;
+  P.bp_wait_limit = 1u << 22;
   P.bp_tmap = encode_lambda_map(&p->bp_tmap, p->lam, p->d.S, p->d.nd, p->d.nang, 128) ? &p->bp_tmap : nullptr;
   P.bp_tmap_wide =
       encode_lambda_map(&p->bp_tmap_wide, p->lam, p->d.S, p->d.nd, p->d.nang, 256) ? &p->bp_tmap_wide : nullptr;
@@ -779,6 +781,17 @@ int gt_set_dual_shape(gt_problem *p, int cfg) {
 }
 
 int gt_get_dual_shape(gt_problem *p) { return p ? p->P.dual_cfg : -1; }
+
+int gt_test_bp_stall(gt_problem *p, int angle, unsigned wait_limit) {
+  if (!p || wait_limit == 0) return set_err(GT_ERR_ARG, "invalid argument");
+  CK(cudaSetDevice(p->device));
+  CK(cudaStreamSynchronize(p->stream));
+  p->P.bp_skip_angle = angle < 0 ? -1 : angle;
+  p->P.bp_wait_limit = wait_limit;
+  if (p->g_one) { cudaGraphExecDestroy(p->g_one); p->g_one = nullptr; }
+  if (p->g_chunk) { cudaGraphExecDestroy(p->g_chunk); p->g_chunk = nullptr; }
+  return GT_OK;
+}
 
 int gt_get_tuning(gt_problem *p, int out[2]) {
   if (!p || !out) return set_err(GT_ERR_ARG, "null argument");

@@ -60,6 +60,8 @@ struct IterParams {
   const void *bp_tmap;   // host copies of the TMA descriptors of lambda for k_bp_tma with
   const void *bp_tmap_wide;  // 128- and 256-slice boxes, or null
   int *err;              // device flag: a kernel gave up a bounded wait (read by gt_synchronize)
+  int bp_skip_angle;     // test hook of k_bp_tma: the copy of this angle is never issued (-1: none)
+  unsigned bp_wait_limit;  // polls of one bounded wait in k_bp_tma
 };
 
 }  // namespace gt

@@ -1476,7 +1476,6 @@ __global__ void __launch_bounds__(256) k_bp(const IterParams P) {
 // that gives up sets P.err, waits (bounded) for its copies in flight and leaves
 // without storing.
 constexpr int BPT_ST = 4, BPT_BINS = 16, BPT_TILE = 8;
-constexpr uint32_t BPT_WAIT_LIMIT = 1u << 22;
 
 // lowest bin the taps of the tile at (x0, y0) can touch for angle o: the floor of
 // the smallest detector coordinate of the tile's corners, minus one for the
@@ -1524,7 +1523,9 @@ __global__ void __launch_bounds__(256) k_bp_tma(const IterParams P, const __grid
     mbar_init_fence();
   }
   __syncthreads();
+  const uint32_t limit = P.bp_wait_limit;
   auto issue = [&](int j) {
+    if (j == P.bp_skip_angle) return;  // test hook: a copy nothing completes
     const int st = j % BPT_ST;
     mbar_arrive_expect_tx(&full[st], BOX);
     tma_load_3d(stage + (size_t)st * BPT_BINS * SC, &tm, &full[st], sb, bp_tile_lo(__ldg(P.ofs + j), x0, y0), j);
@@ -1537,7 +1538,7 @@ __global__ void __launch_bounds__(256) k_bp_tma(const IterParams P, const __grid
   for (int r = 0; r < BPT_TILE; ++r)
 #pragma unroll
     for (int k = 0; k < VW; ++k) acc[r][k] = 0.f;
-  bool tmo = nang > 0 && !mbar_wait_bounded(&full[0], 0, BPT_WAIT_LIMIT);
+  bool tmo = nang > 0 && !mbar_wait_bounded(&full[0], 0, limit);
   int j = 0;
   for (; j < nang; ++j) {
     // every thread has waited for angle j's copy; all have finished angle j - 1
@@ -1582,7 +1583,7 @@ __global__ void __launch_bounds__(256) k_bp_tma(const IterParams P, const __grid
       if (tlo) bpt_tap<VW>(acc[r], q, a0, a1);
       if (thi) bpt_tap<VW>(acc[r], p, b0, b1);
     }
-    if (j + 1 < nang) tmo = !mbar_wait_bounded(&full[(j + 1) % BPT_ST], ((j + 1) / BPT_ST) & 1, BPT_WAIT_LIMIT);
+    if (j + 1 < nang) tmo = !mbar_wait_bounded(&full[(j + 1) % BPT_ST], ((j + 1) / BPT_ST) & 1, limit);
   }
   if (j < nang) {
     // gave up waiting for angle j: flag it, let the copies in flight (angles j ..
@@ -1590,7 +1591,7 @@ __global__ void __launch_bounds__(256) k_bp_tma(const IterParams P, const __grid
     if (threadIdx.x == 0) {
       atomicExch(P.err, 1);
       const int last = min(nang - 1, j >= 2 ? j - 2 + BPT_ST : BPT_ST - 1);
-      for (int a = j; a <= last; ++a) mbar_wait_bounded(&full[a % BPT_ST], (a / BPT_ST) & 1, BPT_WAIT_LIMIT);
+      for (int a = j; a <= last; ++a) mbar_wait_bounded(&full[a % BPT_ST], (a / BPT_ST) & 1, limit);
     }
     return;
   }

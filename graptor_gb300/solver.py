@@ -191,6 +191,38 @@ class Problem:
         g["iterations"] = done
         return g
 
+    # ------------------------------------------------------------------ checkpoint / resume
+    def _state_fields(self):
+        return ("u", "ubar", "p", "pbar", "v", "w", "lambda") if self.regularisation == "TGV" else \
+            ("u", "ubar", "v", "lambda")
+
+    def save(self, path: str) -> None:
+        """Checkpoint the solve to ``path`` (.npz): the problem description, the
+        data, the step-size scalars (operator-norm estimate included) and every
+        iterate, so that :meth:`load` continues the iteration exactly."""
+        self.synchronize()
+        sc = self.scalars
+        fields = {k: self.get(k) for k in self._state_fields()}
+        np.savez(path, dim=self.dim, N=self.N, Nz=self.Nz, C=self.C, nd=self.nd, angles=self.angles,
+                 alpha=self.alpha, mu=self.mu, discrepancy=self.discrepancy, regularisation=self.regularisation,
+                 coupling=self.coupling, stepsize=self.stepsize, normest=sc["normest"],
+                 iterations=sc["iterations"] + getattr(self, "iteration_offset", 0), data=self.get("data"),
+                 **{"state_" + k: v for k, v in fields.items()})
+
+    @classmethod
+    def load(cls, path: str, device: int = 0, stream=None, autotune: bool = True) -> "Problem":
+        """A problem restored from a :meth:`save` checkpoint on ``device``; its
+        next iterations equal those the saved problem would have run."""
+        z = np.load(path, allow_pickle=False)
+        p = cls(int(z["dim"]), int(z["N"]), int(z["Nz"]), int(z["C"]), int(z["nd"]), z["angles"], z["alpha"],
+                z["mu"], str(z["discrepancy"]), str(z["regularisation"]), str(z["coupling"]), float(z["stepsize"]),
+                float(z["normest"]), device, stream, autotune)
+        p.set_data(z["data"], feasible=False)  # stored after the feasibility mask
+        for k in p._state_fields():
+            p.set(k, z["state_" + k])
+        p.iteration_offset = int(z["iterations"])
+        return p
+
     def time_kernels(self, reps: int = 5) -> dict:
         """Mean CUDA-event duration (ms) of each kernel of one iteration."""
         out = (ctypes.c_float * 4)()

@@ -91,6 +91,8 @@ GT_API int gt_set_data(gt_problem *p, const float *f_host, int make_feasible);
 /* Run iters primal-dual iterations (the loop body of 3-D :1194-1221), graph-captured,
  * asynchronous on the problem's stream. */
 GT_API int gt_run(gt_problem *p, int iters);
+/* Wait for the problem's stream; GT_ERR_TIMEOUT if a kernel gave up a bounded wait
+ * since the last call (the iterate is then invalid; the flag is cleared). */
 GT_API int gt_synchronize(gt_problem *p);
 
 /* Copy one state field to / from host memory in the layout described above.
@@ -107,10 +109,19 @@ GT_API int gt_set_tuning(gt_problem *p, int fwd_cfg, int bp_cfg);
 /* Launch shape of the dual kernel: 0 = one slice per thread (every case),
  * 1 = two slices per thread with float2 accesses (3-D TGV, Frobenius or
  * uncorrelated coupling, C <= 4, Nz even), 2 = shape 0 with registers capped
- * for 5 resident blocks per SM (C <= 4).  All give bit-identical iterates; the
+ * for 5 resident blocks per SM (C <= 4), 3-5 = every operand loaded ahead of the
+ * arithmetic (C <= 4; one channel ahead in blocks of 128 threads, all loads
+ * first in blocks of 128 or 64 threads).  All give bit-identical iterates; the
  * autotuner picks the fastest.  gt_get_dual_shape returns the current one. */
 GT_API int gt_set_dual_shape(gt_problem *p, int cfg);
 GT_API int gt_get_dual_shape(gt_problem *p);
+
+/* Test hook of the TMA-staged back projection (back-projection shapes 14, 15):
+ * its next launches never issue the copy of `angle` (a wait nothing completes)
+ * and poll at most `wait_limit` times per wait, so every block gives up, flags
+ * the error and returns; gt_synchronize then reports GT_ERR_TIMEOUT.  angle < 0
+ * restores normal operation (wait_limit 4194304 is the default). */
+GT_API int gt_test_bp_stall(gt_problem *p, int angle, unsigned wait_limit);
 
 /* Scalars the run uses: [0] normest, [1] sigma, [2] tau, [3] iterations run. */
 GT_API int gt_get_scalars(gt_problem *p, double out[4]);

@@ -141,3 +141,28 @@ def test_subsampling_geometry_helpers():
     assert cli.coarse_section(2, 3, 2.0, 5.5, 2.5, 6, "round") == (1, 1)
     assert cli.coarse_section(0, 40, 2.0, 5.5, 2.5, 6, "cover") == (0, 5)
     assert preprocess.pixel_size("x.mrc") == -1.0
+
+
+def test_chunk_shrinks_and_retries_after_out_of_memory(tmp_path, monkeypatch):
+    """Host fault injection: the volume solver reports out-of-memory for chunks of
+    more than 3 slices; the driver shrinks the chunk by 0.7 and retries
+    (Reconstruction_coupled.py:509-536) until every slice is reconstructed."""
+    from graptor_gb300 import GraptorMemoryError
+    from graptor_gb300 import radon_tgv_primal_dual_3d as r3
+    calls = []
+
+    def fake(sino, angles, Parameter, mu, maxiter, ctx, plott, Stepsize, discrepancy, method, reg, Info):
+        nang, nz, nd = np.asarray(sino[0]).shape
+        calls.append(nz)
+        if nz > 3:
+            raise GraptorMemoryError(1, "forced allocation failure")
+        u = np.stack([np.full((nd, nd, nz), 1.0 + c) for c in range(len(sino))])
+        return u, np.ones((len(sino), nang, nz, nd))
+
+    monkeypatch.setattr(r3, "Reconstructionapproach3d", fake)
+    p = _stack(tmp_path, np.abs(np.random.default_rng(3).standard_normal((5, 12, 8))) + 1.0, np.linspace(-60, 60, 5))
+    out = str(tmp_path / "r" / "x")
+    u = cli.main([p, "--SliceLevels", "0", "9", "--Coupling", "frob3d", "--Outfile", out, "--Chunksize", "8",
+                  "--Overlapping", "0", "--Datahandling", "basic", "none", "0.0", "", "0.0"])
+    assert calls[0] == 8 and calls[1] == 5 and max(calls[2:]) <= 3  # 8 -> 5 -> 3 slices at once
+    assert u.shape == (1, 8, 8, 10) and np.all(u == 1.0)

@@ -405,3 +405,54 @@ def test_out_of_memory_is_a_memory_error():
         Problem(3, 4096, 256, 8, 4096, ang, (4, 1), np.ones(8))   # ~18 TB of state
     with Problem(3, 16, 2, 1, 16, ang, (4, 1), [0.2], normest=10.0) as p:  # still usable
         p.set_data(np.ones((2, 30, 16), np.float32)).run(2).synchronize()
+
+
+@pytest.mark.parametrize("reg", ["TGV", "TV"])
+def test_checkpoint_resume_continues_exactly(tmp_path, reg):
+    """save() after 20 iterations, load() into a new problem: its next 10 iterations
+    equal those of the saved problem, bit for bit."""
+    from graptor_gb300 import phantom
+    from graptor_gb300.solver import Problem
+    rng = np.random.default_rng(91)
+    N, Nz, C, nang = 24, 4, 2, 13
+    ang = phantom.angles_deg(nang)
+    f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
+    path = str(tmp_path / "ckpt.npz")
+    with Problem(3, N, Nz, C, N, ang, (4, 1), [0.2, 0.05], regularisation=reg) as p:
+        p.set_data(f).run(20)
+        p.save(path)
+        p.run(10).synchronize()
+        want = {k: p.get(k) for k in p._state_fields()}
+    with Problem.load(path) as q:
+        assert q.iteration_offset == 20
+        q.run(10).synchronize()
+        for k, v in want.items():
+            np.testing.assert_array_equal(q.get(k), v, err_msg=k)
+
+
+def test_bounded_wait_of_tma_back_projection_reports_timeout():
+    """Failure detection without a GPU fault: the TMA back projector is made to wait
+    for a copy that is never issued; every block gives up after a short bounded
+    wait, flags it and returns, gt_synchronize reports GT_ERR_TIMEOUT, and the
+    same problem then runs normally again (the context stays usable)."""
+    from graptor_gb300 import _lib as L
+    from graptor_gb300 import GraptorTimeoutError, phantom
+    from graptor_gb300.solver import Problem
+    rng = np.random.default_rng(92)
+    N, Nz, C, nang = 32, 64, 2, 11  # S = 128: one box width
+    ang = phantom.angles_deg(nang)
+    f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
+    with Problem(3, N, Nz, C, N, ang, (4, 1), [0.2, 0.2], normest=15.0, autotune=False) as p:
+        p.set_data(f)
+        p.set_tuning(0, 14)
+        L.check(L.lib().gt_test_bp_stall(p._h, 5, 4096))
+        p.run(2)
+        with pytest.raises(GraptorTimeoutError):
+            p.synchronize()
+        p.synchronize()  # the flag was cleared
+        L.check(L.lib().gt_test_bp_stall(p._h, -1, 1 << 22))
+        p.set_data(f).run(4).synchronize()
+        got = p.get("u")
+        p.set_tuning(0, 4)
+        p.set_data(f).run(4).synchronize()
+        np.testing.assert_array_equal(got, p.get("u"))
