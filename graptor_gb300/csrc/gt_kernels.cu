@@ -504,6 +504,159 @@ __global__ void __launch_bounds__(NT, MINB) k_dual_pf(const IterParams P) {
   }
 }
 
+// k_dual_cl: k_dual with one thread per voxel-channel (Frobenius or uncorrelated
+// coupling, C <= CP channels).  The CP lanes of a voxel are consecutive lanes of a
+// warp (channel fastest); each loads and updates its own channel (25 loads, all
+// issued before the arithmetic) and the coupled norms gather the other channels'
+// terms by shuffles and add them in k_dual's order (channels ascending, then
+// components), so the iterates are bit-identical to k_dual's.  A thread holds one
+// channel instead of all C, so the kernel runs at several times k_dual's
+// occupancy with every load in flight.
+template <int DIM, bool TGV, int CPL, int CP>
+__global__ void __launch_bounds__(256) k_dual_cl(const IterParams P) {
+  constexpr int K = DIM, KW = DIM == 3 ? 6 : 3;
+  const Dims d = P.d;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long vt = t / CP;  // voxel (pixel, z)
+  const int c = (int)(t - vt * CP);
+  const bool valid = vt < (long long)d.N * d.N * d.Nz;
+  const bool own = valid && c < d.C;  // lanes c >= C of a voxel only take part in the shuffles
+  const int pix = valid ? (int)(vt / d.Nz) : 0;
+  const int z = valid ? (int)(vt - (long long)pix * d.Nz) : 0;
+  const int y = pix / d.N, x = pix - y * d.N;
+  const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
+  const bool hx = x < d.N - 1, hy = y < d.N - 1, hz = z < d.Nz - 1;
+  const bool lx = x > 0, ly = y > 0, lz = z > 0;
+  const float *__restrict__ ub = P.ubar;
+  const float *__restrict__ pb = P.pbar;
+  const size_t i = (size_t)pix * S + (size_t)c * d.Nz + z;
+  const unsigned lane0 = (threadIdx.x & 31) & ~(unsigned)(CP - 1);  // first lane of this voxel's group
+
+  float u0 = 0.f, ux = 0.f, uy = 0.f, uz = 0.f;
+  float p0[K], px[K], py[K], pz[K], vo[K], wo[KW];
+#pragma unroll
+  for (int k = 0; k < K; ++k) { p0[k] = px[k] = py[k] = pz[k] = vo[k] = 0.f; }
+#pragma unroll
+  for (int k = 0; k < KW; ++k) wo[k] = 0.f;
+  if (own) {
+    u0 = ub[i];
+    if (hx) ux = ub[i + S];
+    if (hy) uy = ub[i + rowS];
+    if (DIM == 3 && hz) uz = ub[i + 1];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      vo[k] = P.v[k * vol + i];
+      if (TGV) {
+        p0[k] = pb[k * vol + i];
+        if (lx) px[k] = pb[k * vol + i - S];
+        if (ly) py[k] = pb[k * vol + i - rowS];
+        if (DIM == 3 && lz) pz[k] = pb[k * vol + i - 1];
+      }
+    }
+    if (TGV) {
+#pragma unroll
+      for (int k = 0; k < KW; ++k) wo[k] = P.w[k * vol + i];
+    }
+  }
+
+  const float sigma = P.sigma;
+  float vv[K], ww[KW];
+  {
+    const float mu = -u0;
+    float g[3];
+    g[0] = hx ? mu + ux : 0.f;
+    g[1] = hy ? mu + uy : 0.f;
+    if (DIM == 3) g[2] = (hz ? mu + uz : 0.f) / P.stepsize;
+    float pc[3];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      pc[k] = TGV ? p0[k] : 0.f;
+      vv[k] = vo[k] + sigma * (g[k] - pc[k]);
+    }
+    if (TGV) {
+      float a[3], b[3], cz[3];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        a[k] = lx ? pc[k] - px[k] : 0.f;
+        b[k] = ly ? pc[k] - py[k] : 0.f;
+        if (DIM == 3) cz[k] = (lz ? pc[k] - pz[k] : 0.f) / P.stepsize;
+      }
+      float e[6];
+      if (DIM == 3) {
+        e[0] = a[0]; e[1] = b[1]; e[2] = cz[2];
+        e[3] = 0.5f * (a[1] + b[0]);
+        e[4] = 0.5f * (a[2] + cz[0]);
+        e[5] = 0.5f * (b[2] + cz[1]);
+      } else {
+        e[0] = a[0]; e[1] = b[1];
+        e[2] = 0.5f * (a[1] + b[0]);
+      }
+#pragma unroll
+      for (int k = 0; k < KW; ++k) ww[k] = wo[k] + sigma * e[k];
+    }
+  }
+
+  if (CPL == UNCORR) {
+    float n2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) n2 += vv[k] * vv[k];
+    const float nv = sqrtf(n2) * P.ainv1;
+    if (nv > 1.f) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) vv[k] = vv[k] / nv;
+    }
+    if (TGV) {
+      const float nw = sqrtf(wnorm2<DIM, UNCORR>(ww)) * P.ainv0;
+      if (nw > 1.f) {
+#pragma unroll
+        for (int k = 0; k < KW; ++k) ww[k] = ww[k] / nw;
+      }
+    }
+  } else {  // FROB: the norms over the voxel's channels, summed in k_dual's order
+    const int nC = d.C;
+    float sq[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) sq[k] = vv[k] * vv[k];
+    float n2 = 0.f;
+#pragma unroll
+    for (int cc = 0; cc < CP; ++cc) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const float s = __shfl_sync(0xffffffffu, sq[k], lane0 + cc);
+        if (cc < nC) n2 += s;
+      }
+    }
+    const float nv = sqrtf(n2) * P.ainv1;
+    if (nv > 1.f) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) vv[k] = vv[k] / nv;
+    }
+    if (TGV) {
+      const float wn = wnorm2<DIM, FROB>(ww);
+      float m2 = 0.f;
+#pragma unroll
+      for (int cc = 0; cc < CP; ++cc) {
+        const float s = __shfl_sync(0xffffffffu, wn, lane0 + cc);
+        if (cc < nC) m2 += s;
+      }
+      const float nw = sqrtf(m2) * P.ainv0;
+      if (nw > 1.f) {
+#pragma unroll
+        for (int k = 0; k < KW; ++k) ww[k] = ww[k] / nw;
+      }
+    }
+  }
+
+  if (own) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) P.v[k * vol + i] = vv[k];
+    if (TGV) {
+#pragma unroll
+      for (int k = 0; k < KW; ++k) P.w[k * vol + i] = ww[k];
+    }
+  }
+}
+
 // k_dual_z2: k_dual for 3-D TGV with Frobenius or uncorrelated coupling, a thread
 // per (pixel, pair of consecutive slices z0, z0+1): every field is read and
 // written as float2 (half the load instructions of k_dual), in two phases (v,
@@ -2191,8 +2344,10 @@ bool dual_z2_ok(const IterParams &P, int tgv, int cpl) {
 // dual launch shapes: 0 k_dual, 1 k_dual_z2 (where dual_z2_ok; else the same as 0),
 // 2 k_dual with registers capped for 5 resident blocks (C <= 4; else as 0),
 // 3-5 k_dual_pf: loads one channel ahead in 128-thread blocks (3), all loads first
-// in 128-thread (4) or 64-thread (5) blocks (C <= 4; else as 0)
-int num_dual_configs(const IterParams &P) { return P.d.C <= 4 ? 6 : 1; }
+// in 128-thread (4) or 64-thread (5) blocks (C <= 4; else as 0),
+// 6 k_dual_cl: one thread per voxel-channel (Frobenius / uncorrelated, C <= 4; else as 0)
+int num_dual_configs(const IterParams &P) { return P.d.C <= 4 ? 7 : 1; }
+bool dual_cl_ok(const IterParams &P, int cpl) { return cpl != NUCL && P.d.C <= 4; }
 
 template <int CPL>
 static void launch_dual_z2(const IterParams &P, cudaStream_t st) {
@@ -2222,7 +2377,16 @@ static cudaError_t launch_dual_c(const IterParams &P, cudaStream_t st) {
     launch_dual_z2<CPL == NUCL ? FROB : CPL>(P, st);
     return cudaGetLastError();
   }
-  if (P.dual_cfg >= 3 && C <= 4) {  // operands loaded ahead of the arithmetic
+  if (P.dual_cfg == 6 && C <= 4 && CPL != NUCL) {  // one thread per voxel-channel
+    constexpr int Q = CPL == NUCL ? FROB : CPL;
+    const long long cp = C <= 1 ? 1 : (C <= 2 ? 2 : 4);
+    const unsigned gc = blocks_for(n * cp, 256);
+    if (cp == 1) k_dual_cl<DIM, TGV, Q, 1><<<gc, 256, 0, st>>>(P);
+    else if (cp == 2) k_dual_cl<DIM, TGV, Q, 2><<<gc, 256, 0, st>>>(P);
+    else k_dual_cl<DIM, TGV, Q, 4><<<gc, 256, 0, st>>>(P);
+    return cudaGetLastError();
+  }
+  if (P.dual_cfg >= 3 && P.dual_cfg <= 5 && C <= 4) {  // operands loaded ahead of the arithmetic
     if (P.dual_cfg == 3) launch_dual_pf<DIM, TGV, CPL, 5, 128, 1>(P, st);  // one channel ahead, 96 registers
     else if (P.dual_cfg == 4) launch_dual_pf<DIM, TGV, CPL, 4, 128>(P, st);  // all channels, 128 registers
     else launch_dual_pf<DIM, TGV, CPL, 8, 64>(P, st);                        // as 4 in 64-thread blocks
