@@ -59,6 +59,7 @@ int num_proj_configs(int S, int which);
 bool dual_z2_ok(const IterParams &P, int tgv, int cpl);
 int num_dual_configs(const IterParams &P);
 bool dual_cl_ok(const IterParams &P, int cpl);
+bool dual_cl2_ok(const IterParams &P, int cpl);
 int gap_blocks(const IterParams &P);
 cudaError_t launch_gap_pass1(const IterParams &P, int disc, int tgv, int cpl, float *vt, double *part, int nb,
                              cudaStream_t st);
@@ -772,7 +773,7 @@ int gt_set_dual_shape(gt_problem *p, int cfg) {
   if (!p) return set_err(GT_ERR_ARG, "null argument");
   const int n = gt::num_dual_configs(p->P);
   if (cfg < 0 || cfg >= n || (cfg == 1 && !gt::dual_z2_ok(p->P, p->reg == GT_TGV, p->cpl)) ||
-      (cfg == 6 && !gt::dual_cl_ok(p->P, p->cpl)))
+      (cfg == 6 && !gt::dual_cl_ok(p->P, p->cpl)) || (cfg == 7 && !gt::dual_cl2_ok(p->P, p->cpl)))
     return set_err(GT_ERR_ARG, "dual launch shape %d not available here", cfg);
   CK(cudaSetDevice(p->device));
   CK(cudaStreamSynchronize(p->stream));

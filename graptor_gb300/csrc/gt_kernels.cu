@@ -657,13 +657,168 @@ __global__ void __launch_bounds__(256) k_dual_cl(const IterParams P) {
   }
 }
 
+__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ void st2(float *p, float a, float b) { *reinterpret_cast<float2 *>(p) = make_float2(a, b); }
+
+// k_dual_cl2: k_dual_cl for two consecutive slices z0, z0 + 1 of one channel per
+// thread (3-D, Nz even): the fields of both slices move as one float2, the slice
+// neighbours outside the pair as one float each.  Per slice the arithmetic and the
+// shuffle order are k_dual_cl's, so the iterates are bit-identical to k_dual's.
+template <bool TGV, int CPL, int CP>
+__global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
+  constexpr int K = 3, KW = 6;
+  const Dims d = P.d;
+  const int nz2 = d.Nz >> 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long vt = t / CP;  // (pixel, slice pair)
+  const int c = (int)(t - vt * CP);
+  const bool valid = vt < (long long)d.N * d.N * nz2;
+  const bool own = valid && c < d.C;
+  const int pix = valid ? (int)(vt / nz2) : 0;
+  const int z0 = valid ? 2 * (int)(vt - (long long)pix * nz2) : 0;
+  const int y = pix / d.N, x = pix - y * d.N;
+  const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
+  const bool hx = x < d.N - 1, hy = y < d.N - 1;
+  const bool lx = x > 0, ly = y > 0;
+  const bool hz[2] = {true, z0 + 1 < d.Nz - 1}, lz[2] = {z0 > 0, true};
+  const float *__restrict__ ub = P.ubar;
+  const float *__restrict__ pb = P.pbar;
+  const size_t i = (size_t)pix * S + (size_t)c * d.Nz + z0;
+  const unsigned lane0 = (threadIdx.x & 31) & ~(unsigned)(CP - 1);
+
+  float2 u0 = make_float2(0.f, 0.f), ux = u0, uy = u0;
+  float uz1 = 0.f;  // ubar at z0 + 2
+  float2 p0[K], px[K], py[K], vo[K], wo[KW];
+  float pzm[K];  // pbar at z0 - 1
+#pragma unroll
+  for (int k = 0; k < K; ++k) { p0[k] = px[k] = py[k] = vo[k] = u0; pzm[k] = 0.f; }
+#pragma unroll
+  for (int k = 0; k < KW; ++k) wo[k] = u0;
+  if (own) {
+    u0 = ld2(ub + i);
+    if (hx) ux = ld2(ub + i + S);
+    if (hy) uy = ld2(ub + i + rowS);
+    if (hz[1]) uz1 = ub[i + 2];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      vo[k] = ld2(P.v + k * vol + i);
+      if (TGV) {
+        p0[k] = ld2(pb + k * vol + i);
+        if (lx) px[k] = ld2(pb + k * vol + i - S);
+        if (ly) py[k] = ld2(pb + k * vol + i - rowS);
+        if (lz[0]) pzm[k] = pb[k * vol + i - 1];
+      }
+    }
+    if (TGV) {
+#pragma unroll
+      for (int k = 0; k < KW; ++k) wo[k] = ld2(P.w + k * vol + i);
+    }
+  }
+
+  const float sigma = P.sigma;
+  float vv[2][K], ww[2][KW];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float uc = h ? u0.y : u0.x, uxn = h ? ux.y : ux.x, uyn = h ? uy.y : uy.x;
+    const float uzn = h ? uz1 : u0.y;
+    const float mu = -uc;
+    float g[3];
+    g[0] = hx ? mu + uxn : 0.f;
+    g[1] = hy ? mu + uyn : 0.f;
+    g[2] = (hz[h] ? mu + uzn : 0.f) / P.stepsize;
+    float pc[3];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      pc[k] = TGV ? (h ? p0[k].y : p0[k].x) : 0.f;
+      vv[h][k] = (h ? vo[k].y : vo[k].x) + sigma * (g[k] - pc[k]);
+    }
+    if (TGV) {
+      float a[3], b[3], cz[3];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        a[k] = lx ? pc[k] - (h ? px[k].y : px[k].x) : 0.f;
+        b[k] = ly ? pc[k] - (h ? py[k].y : py[k].x) : 0.f;
+        cz[k] = (lz[h] ? pc[k] - (h ? p0[k].x : pzm[k]) : 0.f) / P.stepsize;
+      }
+      float e[6];
+      e[0] = a[0]; e[1] = b[1]; e[2] = cz[2];
+      e[3] = 0.5f * (a[1] + b[0]);
+      e[4] = 0.5f * (a[2] + cz[0]);
+      e[5] = 0.5f * (b[2] + cz[1]);
+#pragma unroll
+      for (int k = 0; k < KW; ++k) ww[h][k] = (h ? wo[k].y : wo[k].x) + sigma * e[k];
+    }
+  }
+
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    if (CPL == UNCORR) {
+      float n2 = 0.f;
+#pragma unroll
+      for (int k = 0; k < K; ++k) n2 += vv[h][k] * vv[h][k];
+      const float nv = sqrtf(n2) * P.ainv1;
+      if (nv > 1.f) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) vv[h][k] = vv[h][k] / nv;
+      }
+      if (TGV) {
+        const float nw = sqrtf(wnorm2<3, UNCORR>(ww[h])) * P.ainv0;
+        if (nw > 1.f) {
+#pragma unroll
+          for (int k = 0; k < KW; ++k) ww[h][k] = ww[h][k] / nw;
+        }
+      }
+    } else {
+      const int nC = d.C;
+      float sq[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) sq[k] = vv[h][k] * vv[h][k];
+      float n2 = 0.f;
+#pragma unroll
+      for (int cc = 0; cc < CP; ++cc) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const float s = __shfl_sync(0xffffffffu, sq[k], lane0 + cc);
+          if (cc < nC) n2 += s;
+        }
+      }
+      const float nv = sqrtf(n2) * P.ainv1;
+      if (nv > 1.f) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) vv[h][k] = vv[h][k] / nv;
+      }
+      if (TGV) {
+        const float wn = wnorm2<3, FROB>(ww[h]);
+        float m2 = 0.f;
+#pragma unroll
+        for (int cc = 0; cc < CP; ++cc) {
+          const float s = __shfl_sync(0xffffffffu, wn, lane0 + cc);
+          if (cc < nC) m2 += s;
+        }
+        const float nw = sqrtf(m2) * P.ainv0;
+        if (nw > 1.f) {
+#pragma unroll
+          for (int k = 0; k < KW; ++k) ww[h][k] = ww[h][k] / nw;
+        }
+      }
+    }
+  }
+
+  if (own) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) st2(P.v + k * vol + i, vv[0][k], vv[1][k]);
+    if (TGV) {
+#pragma unroll
+      for (int k = 0; k < KW; ++k) st2(P.w + k * vol + i, ww[0][k], ww[1][k]);
+    }
+  }
+}
+
 // k_dual_z2: k_dual for 3-D TGV with Frobenius or uncorrelated coupling, a thread
 // per (pixel, pair of consecutive slices z0, z0+1): every field is read and
 // written as float2 (half the load instructions of k_dual), in two phases (v,
 // then w) to bound the registers.  Every value is computed by the same
 // operations as in k_dual, so the iterates are bit-identical.  Needs Nz even.
-__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
-__device__ __forceinline__ void st2(float *p, float a, float b) { *reinterpret_cast<float2 *>(p) = make_float2(a, b); }
 
 template <int CPL, int CMAX>
 __global__ void __launch_bounds__(256) k_dual_z2(const IterParams P) {
@@ -2345,9 +2500,11 @@ bool dual_z2_ok(const IterParams &P, int tgv, int cpl) {
 // 2 k_dual with registers capped for 5 resident blocks (C <= 4; else as 0),
 // 3-5 k_dual_pf: loads one channel ahead in 128-thread blocks (3), all loads first
 // in 128-thread (4) or 64-thread (5) blocks (C <= 4; else as 0),
-// 6 k_dual_cl: one thread per voxel-channel (Frobenius / uncorrelated, C <= 4; else as 0)
-int num_dual_configs(const IterParams &P) { return P.d.C <= 4 ? 7 : 1; }
+// 6 k_dual_cl: one thread per voxel-channel (Frobenius / uncorrelated, C <= 4; else as 0),
+// 7 k_dual_cl2: one thread per channel and slice pair (3-D, Nz even; else as 6)
+int num_dual_configs(const IterParams &P) { return P.d.C <= 4 ? 8 : 1; }
 bool dual_cl_ok(const IterParams &P, int cpl) { return cpl != NUCL && P.d.C <= 4; }
+bool dual_cl2_ok(const IterParams &P, int cpl) { return dual_cl_ok(P, cpl) && P.d.dim == 3 && P.d.Nz % 2 == 0; }
 
 template <int CPL>
 static void launch_dual_z2(const IterParams &P, cudaStream_t st) {
@@ -2377,7 +2534,16 @@ static cudaError_t launch_dual_c(const IterParams &P, cudaStream_t st) {
     launch_dual_z2<CPL == NUCL ? FROB : CPL>(P, st);
     return cudaGetLastError();
   }
-  if (P.dual_cfg == 6 && C <= 4 && CPL != NUCL) {  // one thread per voxel-channel
+  if (DIM == 3 && P.dual_cfg == 7 && C <= 4 && CPL != NUCL && P.d.Nz % 2 == 0) {  // ... and slice pair
+    constexpr int Q = CPL == NUCL ? FROB : CPL;
+    const long long cp = C <= 1 ? 1 : (C <= 2 ? 2 : 4);
+    const unsigned gc = blocks_for((long long)P.d.N * P.d.N * (P.d.Nz / 2) * cp, 256);
+    if (cp == 1) k_dual_cl2<TGV, Q, 1><<<gc, 256, 0, st>>>(P);
+    else if (cp == 2) k_dual_cl2<TGV, Q, 2><<<gc, 256, 0, st>>>(P);
+    else k_dual_cl2<TGV, Q, 4><<<gc, 256, 0, st>>>(P);
+    return cudaGetLastError();
+  }
+  if (P.dual_cfg >= 6 && C <= 4 && CPL != NUCL) {  // one thread per voxel-channel
     constexpr int Q = CPL == NUCL ? FROB : CPL;
     const long long cp = C <= 1 ? 1 : (C <= 2 ? 2 : 4);
     const unsigned gc = blocks_for(n * cp, 256);

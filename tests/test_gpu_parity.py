@@ -256,7 +256,10 @@ def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg):
     f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
     got = []
     z2 = dim == 3 and reg == "TGV" and cpl != "NUCL"
-    shapes = (0, 1, 2, 3, 4, 5, 6) if z2 else ((0, 2, 3, 4, 5) if cpl == "NUCL" else (0, 2, 3, 4, 5, 6))
+    if cpl == "NUCL":
+        shapes = (0, 2, 3, 4, 5)
+    else:
+        shapes = (0, 1, 2, 3, 4, 5, 6, 7) if z2 else ((0, 2, 3, 4, 5, 6, 7) if dim == 3 else (0, 2, 3, 4, 5, 6))
     fields = ("u", "v", "w", "p") if reg == "TGV" else ("u", "v")
     with Problem(dim, N, Nz, C, N, ang, (4, 1), [0.3] * C, regularisation=reg, coupling=cpl, normest=17.0,
                  stepsize=2.0) as p:
@@ -266,19 +269,25 @@ def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg):
             p.run(9).synchronize()
             got.append({k: p.get(k) for k in fields})
         with pytest.raises(ValueError):
-            p.set_dual_shape(7)
+            p.set_dual_shape(8)
         if not z2:
             with pytest.raises(ValueError):
                 p.set_dual_shape(1)
         if cpl == "NUCL":
             with pytest.raises(ValueError):
                 p.set_dual_shape(6)
+        if cpl == "NUCL" or dim == 2:
+            with pytest.raises(ValueError):
+                p.set_dual_shape(7)
     for g in got[1:]:
         for k in got[0]:
             np.testing.assert_array_equal(g[k], got[0][k], err_msg=k)
-    with Problem(3, N, 5, C, N, ang, (4, 1), [0.3] * C, normest=17.0) as q:  # odd Nz: no two-slice shape
+    with Problem(3, N, 5, C, N, ang, (4, 1), [0.3] * C, normest=17.0) as q:  # odd Nz: no two-slice shapes
         with pytest.raises(ValueError):
             q.set_dual_shape(1)
+        if C <= 4:
+            with pytest.raises(ValueError):
+                q.set_dual_shape(7)
 
 
 @pytest.mark.parametrize("disc", ["KL", "L2"])
