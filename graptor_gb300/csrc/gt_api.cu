@@ -773,7 +773,8 @@ int gt_set_dual_shape(gt_problem *p, int cfg) {
   if (!p) return set_err(GT_ERR_ARG, "null argument");
   const int n = gt::num_dual_configs(p->P);
   if (cfg < 0 || cfg >= n || (cfg == 1 && !gt::dual_z2_ok(p->P, p->reg == GT_TGV, p->cpl)) ||
-      (cfg == 6 && !gt::dual_cl_ok(p->P, p->cpl)) || (cfg == 7 && !gt::dual_cl2_ok(p->P, p->cpl)))
+      ((cfg == 6 || cfg == 8) && !gt::dual_cl_ok(p->P, p->cpl)) ||
+      ((cfg == 7 || cfg == 9) && !gt::dual_cl2_ok(p->P, p->cpl)))
     return set_err(GT_ERR_ARG, "dual launch shape %d not available here", cfg);
   CK(cudaSetDevice(p->device));
   CK(cudaStreamSynchronize(p->stream));

@@ -2501,10 +2501,12 @@ bool dual_z2_ok(const IterParams &P, int tgv, int cpl) {
 // 3-5 k_dual_pf: loads one channel ahead in 128-thread blocks (3), all loads first
 // in 128-thread (4) or 64-thread (5) blocks (C <= 4; else as 0),
 // 6 k_dual_cl: one thread per voxel-channel (Frobenius / uncorrelated, C <= 4; else as 0),
-// 7 k_dual_cl2: one thread per channel and slice pair (3-D, Nz even; else as 6)
-int num_dual_configs(const IterParams &P) { return P.d.C <= 4 ? 8 : 1; }
+// 7 k_dual_cl2: one thread per channel and slice pair (3-D, Nz even; else as 6),
+// 8, 9: shapes 6, 7 in blocks of 128 threads
+int num_dual_configs(const IterParams &P) { return P.d.C <= 4 ? 10 : 1; }
 bool dual_cl_ok(const IterParams &P, int cpl) { return cpl != NUCL && P.d.C <= 4; }
 bool dual_cl2_ok(const IterParams &P, int cpl) { return dual_cl_ok(P, cpl) && P.d.dim == 3 && P.d.Nz % 2 == 0; }
+// shape 7 or 9 where it is not available falls back to 6 or 8 (one slice per thread)
 
 template <int CPL>
 static void launch_dual_z2(const IterParams &P, cudaStream_t st) {
@@ -2543,13 +2545,23 @@ static cudaError_t launch_dual_c(const IterParams &P, cudaStream_t st) {
     else k_dual_cl2<TGV, Q, 4><<<gc, 256, 0, st>>>(P);
     return cudaGetLastError();
   }
+  if (DIM == 3 && P.dual_cfg == 9 && C <= 4 && CPL != NUCL && P.d.Nz % 2 == 0) {
+    constexpr int Q = CPL == NUCL ? FROB : CPL;
+    const long long cp = C <= 1 ? 1 : (C <= 2 ? 2 : 4);
+    const unsigned gc = blocks_for((long long)P.d.N * P.d.N * (P.d.Nz / 2) * cp, 128);
+    if (cp == 1) k_dual_cl2<TGV, Q, 1><<<gc, 128, 0, st>>>(P);
+    else if (cp == 2) k_dual_cl2<TGV, Q, 2><<<gc, 128, 0, st>>>(P);
+    else k_dual_cl2<TGV, Q, 4><<<gc, 128, 0, st>>>(P);
+    return cudaGetLastError();
+  }
   if (P.dual_cfg >= 6 && C <= 4 && CPL != NUCL) {  // one thread per voxel-channel
     constexpr int Q = CPL == NUCL ? FROB : CPL;
     const long long cp = C <= 1 ? 1 : (C <= 2 ? 2 : 4);
-    const unsigned gc = blocks_for(n * cp, 256);
-    if (cp == 1) k_dual_cl<DIM, TGV, Q, 1><<<gc, 256, 0, st>>>(P);
-    else if (cp == 2) k_dual_cl<DIM, TGV, Q, 2><<<gc, 256, 0, st>>>(P);
-    else k_dual_cl<DIM, TGV, Q, 4><<<gc, 256, 0, st>>>(P);
+    const int nt = (P.dual_cfg == 8 || P.dual_cfg == 9) ? 128 : 256;
+    const unsigned gc = blocks_for(n * cp, nt);
+    if (cp == 1) k_dual_cl<DIM, TGV, Q, 1><<<gc, nt, 0, st>>>(P);
+    else if (cp == 2) k_dual_cl<DIM, TGV, Q, 2><<<gc, nt, 0, st>>>(P);
+    else k_dual_cl<DIM, TGV, Q, 4><<<gc, nt, 0, st>>>(P);
     return cudaGetLastError();
   }
   if (P.dual_cfg >= 3 && P.dual_cfg <= 5 && C <= 4) {  // operands loaded ahead of the arithmetic

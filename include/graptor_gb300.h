@@ -113,8 +113,9 @@ GT_API int gt_set_tuning(gt_problem *p, int fwd_cfg, int bp_cfg);
  * arithmetic (C <= 4; one channel ahead in blocks of 128 threads, all loads
  * first in blocks of 128 or 64 threads), 6 = one thread per voxel-channel and
  * 7 = per channel and slice pair (Frobenius or uncorrelated coupling, C <= 4;
- * 7 needs 3-D and Nz even).  All give bit-identical iterates; the autotuner
- * picks the fastest.  gt_get_dual_shape returns the current one. */
+ * 7 needs 3-D and Nz even), 8, 9 = shapes 6, 7 in blocks of 128 threads.  All
+ * give bit-identical iterates; the autotuner picks the fastest.
+ * gt_get_dual_shape returns the current one. */
 GT_API int gt_set_dual_shape(gt_problem *p, int cfg);
 GT_API int gt_get_dual_shape(gt_problem *p);
 

@@ -258,8 +258,10 @@ def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg):
     z2 = dim == 3 and reg == "TGV" and cpl != "NUCL"
     if cpl == "NUCL":
         shapes = (0, 2, 3, 4, 5)
+    elif dim == 2:
+        shapes = (0, 2, 3, 4, 5, 6, 8)
     else:
-        shapes = (0, 1, 2, 3, 4, 5, 6, 7) if z2 else ((0, 2, 3, 4, 5, 6, 7) if dim == 3 else (0, 2, 3, 4, 5, 6))
+        shapes = (0, 1, 2, 3, 4, 5, 6, 7, 8, 9) if z2 else (0, 2, 3, 4, 5, 6, 7, 8, 9)
     fields = ("u", "v", "w", "p") if reg == "TGV" else ("u", "v")
     with Problem(dim, N, Nz, C, N, ang, (4, 1), [0.3] * C, regularisation=reg, coupling=cpl, normest=17.0,
                  stepsize=2.0) as p:
@@ -269,16 +271,18 @@ def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg):
             p.run(9).synchronize()
             got.append({k: p.get(k) for k in fields})
         with pytest.raises(ValueError):
-            p.set_dual_shape(8)
+            p.set_dual_shape(10)
         if not z2:
             with pytest.raises(ValueError):
                 p.set_dual_shape(1)
         if cpl == "NUCL":
-            with pytest.raises(ValueError):
-                p.set_dual_shape(6)
+            for sh in (6, 8):
+                with pytest.raises(ValueError):
+                    p.set_dual_shape(sh)
         if cpl == "NUCL" or dim == 2:
-            with pytest.raises(ValueError):
-                p.set_dual_shape(7)
+            for sh in (7, 9):
+                with pytest.raises(ValueError):
+                    p.set_dual_shape(sh)
     for g in got[1:]:
         for k in got[0]:
             np.testing.assert_array_equal(g[k], got[0][k], err_msg=k)
@@ -286,8 +290,9 @@ def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg):
         with pytest.raises(ValueError):
             q.set_dual_shape(1)
         if C <= 4:
-            with pytest.raises(ValueError):
-                q.set_dual_shape(7)
+            for sh in (7, 9):
+                with pytest.raises(ValueError):
+                    q.set_dual_shape(sh)
 
 
 @pytest.mark.parametrize("disc", ["KL", "L2"])
