@@ -435,6 +435,66 @@ WARM = dict(N=128, Nz=32, C=2, nang=71, pre=500, tol=1e-2, check_every=100, max_
             weights=os.path.join(ROOT, "graptor_gb300", "weights", "unet_tgv_kl_c2_p500.npz"))
 
 
+def run_unet(args, rank, world, local):
+    """The warm-start network's forward pass (3-level 3-D U-Net 16-32-64, 2 channels in
+    and out, batch 2 of 32x128x128, bfloat16 activations): convolutions with
+    16k input and output channels on the tensor cores (tcgen05), the others on
+    the CUDA cores; the same pass with every convolution on the CUDA cores beside it."""
+    import torch
+
+    from graptor_gb300 import _lib as L
+    from graptor_gb300.warmstart import UNet3D, unet_layers
+    torch.cuda.set_device(local)
+    B, C, D, H, Wd = 2, 2, 32, 128, 128
+    net = UNet3D(C, C, residual=C, device=local)
+    net.refresh()
+    x = torch.randn((B, C, D, H, Wd), device="cuda", generator=torch.Generator("cuda").manual_seed(rank)).to(
+        torch.bfloat16)
+    out = torch.zeros((B, C, D, H, Wd), device="cuda")
+    # algorithmic FLOPs of the convolutions (2 per multiply-add), by level
+    flops = tc_flops = 0.0
+    levels = {"enc1a": 0, "enc1b": 0, "enc2a": 1, "enc2b": 1, "bota": 2, "botb": 2, "dec2a": 1, "dec2b": 1,
+              "dec1a": 0, "dec1b": 0, "head": 0}
+    for name, ci, co, k in unet_layers(C, C):
+        vox = B * D * H * Wd / 8 ** levels[name]
+        fl = 2.0 * vox * ci * co * k ** 3
+        flops += fl
+        if ci % 16 == 0 and co % 16 == 0:
+            tc_flops += fl
+    times = {}
+    for tc in (0, 1):
+        L.check(L.lib().gt_nn_set_tensor_cores(tc))
+        for _ in range(args.warmup):
+            net.forward(x, out)
+        torch.cuda.synchronize()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            net.forward(x, out)
+        e1.record()
+        e1.synchronize()
+        L.check(L.lib().gt_nn_check())
+        times[tc] = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
+    L.check(L.lib().gt_nn_set_tensor_cores(1))
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peak, kind = float(json.load(fh)["bf16_tflops"]), "measured"
+    except Exception:
+        peak, kind = 1900.0, "fallback"
+    if rank != 0:
+        return None
+    ms = times[1]
+    return {"metric": "unet-forward/s", "value": world * 1e3 / ms, "unit": "forward/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic",
+            "config": {"workload": "warm-start U-Net 16-32-64 forward, batch 2 x 2 channels x 32x128x128",
+                       "conv_gflop": flops / 1e9, "tensor_core_gflop": tc_flops / 1e9},
+            "cuda_cores_only_ms": times[0],
+            "roofline": {"bound": "tensor", "achieved": flops / (ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                         "frac": flops / (ms / 1e3) / 1e12 / peak, "peak_source": kind, "traffic": None}}
+
+
 def run_warmstart(args, rank, world, local):
     """Time to relative primal-dual gap <= tol on held-out seeded problems
     (3-D TGV-KL, FROB, 2 channels, 128^2 x 32, 71 angles): the plain solver
@@ -546,7 +606,7 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="image side (default 256); profiler captures")
     ap.add_argument("--nang", type=int, default=None,
                     help="projection angles (default 71; the 768^2 x 384 large run uses 141)")
-    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart"],
+    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart", "unet"],
                     help="coupled3d: the 3-D 4-channel workload (default); batched: 64 uneven problems; "
                          "warmstart: time to gap, cold start against learned warm start + batch")
     ap.add_argument("--batch", type=int, default=64, help="problems per rank for --workload batched")
@@ -572,6 +632,8 @@ def main():
         out = run_batched(args, rank, world, local)
     elif args.workload == "warmstart":
         out = run_warmstart(args, rank, world, local)
+    elif args.workload == "unet":
+        out = run_unet(args, rank, world, local)
     else:
         from oracle import oracle as O
         O.build()  # the CPU-baseline leg needs the oracle library (built before any GPU work)

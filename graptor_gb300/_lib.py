@@ -113,6 +113,8 @@ _SIGS = {
     "gt_nn_adam": (ctypes.c_int, [_P, _P, _P, _P, _P, _LL, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float, _I, _P]),
     "gt_nn_cast": (ctypes.c_int, [_P, _I, _P, _LL, _P]),
+    "gt_nn_set_tensor_cores": (ctypes.c_int, [_I]),
+    "gt_nn_check": (ctypes.c_int, []),
     "gt_subs_create": (ctypes.c_int, [ctypes.POINTER(GtSubsDesc), ctypes.POINTER(ctypes.c_void_p)]),
     "gt_subs_destroy": (None, [_P]),
     "gt_subs_set_data": (ctypes.c_int, [_P, _P, _P, _I]),

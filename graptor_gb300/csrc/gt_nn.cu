@@ -6,7 +6,9 @@
 // stride 1, zero padding (k-1)/2.  Outputs can be written at a channel offset of
 // a wider tensor (the U-Net's skip concatenation is free) and can accumulate.
 //
-//   gt_nn_conv3d        forward (and, with transformed weights, the data gradient)
+//   gt_nn_conv3d        forward (and, with transformed weights, the data gradient); BF16
+//                       inputs with 16k in and out channels run on the tensor cores
+//                       (k_conv3d_tc: tcgen05 MMA, accumulator in tensor memory)
 //   gt_nn_flip_weights  w[co][ci][t] -> w'[ci][co][K3-1-t]   (data-gradient weights)
 //   gt_nn_conv3d_wgrad  weight gradient as a split-K GEMM  dW = dY * im2col(X)^T
 //   gt_nn_bias_grad, gt_nn_relu_bwd, gt_nn_pool2 / _bwd, gt_nn_up2 / _bwd,
@@ -15,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "graptor_gb300.h"
+#include "gt_tc.cuh"
 
 namespace {
 
@@ -115,6 +118,141 @@ __global__ void __launch_bounds__(128) k_conv3d(const TI *__restrict__ x, int Ci
     }
   }
 }
+
+// ---------------------------------------------------------------------------
+// forward convolution on the tensor cores: implicit GEMM Y[voxel][co] =
+// sum over (tap, ci) of X[voxel + tap][ci] W[co][ci][tap].  A block owns 128
+// consecutive voxels (M = 128, one TMEM lane each) and all Co output channels
+// (N = Co, one FP32 TMEM column each).  K runs over taps x 16-channel chunks;
+// per chunk the 128 x 16 BF16 slice of im2col(X) (each thread gathers its voxel's
+// 16 channels) and the Co x 16 BF16 weights are written to shared memory as
+// 8-row x 16-byte core matrices, double-buffered, and one thread issues one
+// tcgen05.mma (K = 16) and commits it to the stage's mbarrier; a stage is
+// rewritten only after the MMA that read it has completed.  The epilogue reads
+// the accumulator from tensor memory (tcgen05.ld, warp w = lanes 32w..32w+31),
+// adds bias, the existing output (accumulate) and applies ReLU.  Waits are
+// bounded: a block that gives up flags g_nn_err, never leaves tensor memory
+// allocated, and stores nothing.
+// ---------------------------------------------------------------------------
+__device__ int g_nn_err;
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 20;
+
+__device__ __forceinline__ uint32_t bf16_pair(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+template <class TO, int KS>
+__global__ void __launch_bounds__(128) k_conv3d_tc(const __nv_bfloat16 *__restrict__ x, int Ci, int Cx, int x_off,
+                                                   const __nv_bfloat16 *__restrict__ w,
+                                                   const float *__restrict__ bias, TO *__restrict__ y, int Co, int Cy,
+                                                   int co_off, Shape s, int relu, int accumulate) {
+  constexpr int K3 = KS * KS * KS, R = KS / 2;
+  constexpr int ABYTES = 128 * 16 * 2, BBYTES = 256 * 16 * 2;
+  __shared__ __align__(1024) uint8_t sA[2][ABYTES];
+  __shared__ __align__(1024) uint8_t sB[2][BBYTES];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const long long nvox = (long long)s.B * s.D * s.H * s.W;
+  const long long vox = (long long)blockIdx.x * 128 + tid;
+  const bool active = vox < nvox;
+  int b = 0, d = 0, h = 0, wx = 0;
+  if (active) {
+    long long r = vox;
+    wx = (int)(r % s.W); r /= s.W;
+    h = (int)(r % s.H); r /= s.H;
+    d = (int)(r % s.D); b = (int)(r / s.D);
+  }
+  const size_t plane = (size_t)s.H * s.W, vol = plane * s.D;
+  const uint32_t ncols = Co <= 32 ? 32u : (Co <= 64 ? 64u : (Co <= 128 ? 128u : 256u));
+  if (warp == 0) gt::tmem_alloc(&tslot, ncols);
+  if (tid == 0) {
+    gt::mbar_init(&bar[0], 1);
+    gt::mbar_init(&bar[1], 1);
+    gt::mbar_init_fence();
+  }
+  gt::tc_fence_before();
+  __syncthreads();
+  gt::tc_fence_after();
+  const uint32_t tmem = tslot;
+  const int nci = Ci / 16, nk = K3 * nci;
+  const uint32_t idesc = gt::tc_idesc_bf16_f32(128, Co);
+  bool ok = true;
+  int issued = 0;  // MMAs issued (their commits complete the stages' phases in order)
+  for (int q = 0; q < nk; ++q) {
+    const int st = q & 1;
+    if (q >= 2) {  // the MMA that read this stage (chunk q - 2) must have completed
+      const bool done = gt::mbar_wait_bounded(&bar[st], ((q - 2) >> 1) & 1, TC_WAIT_LIMIT);
+      if (__syncthreads_or(!done)) { ok = false; break; }
+    }
+    const int t = q / nci, ci0 = (q - t * nci) * 16;
+    {  // A: this thread's voxel, channels ci0 .. ci0 + 15 at tap t
+      const int kd = t / (KS * KS), kh = (t / KS) % KS, kw = t % KS;
+      const int dd = d + kd - R, hh = h + kh - R, w2 = wx + kw - R;
+      const bool in = active && dd >= 0 && dd < s.D && hh >= 0 && hh < s.H && w2 >= 0 && w2 < s.W;
+      uint32_t pk[8];
+      if (in) {
+        const __nv_bfloat16 *xp = x + ((size_t)b * Cx + x_off + ci0) * vol + (size_t)dd * plane + (size_t)hh * s.W + w2;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) pk[j] = bf16_pair(xp[(size_t)(2 * j) * vol], xp[(size_t)(2 * j + 1) * vol]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) pk[j] = 0u;
+      }
+      uint8_t *row = sA[st] + (tid >> 3) * 256 + (tid & 7) * 16;
+      *reinterpret_cast<uint4 *>(row) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      *reinterpret_cast<uint4 *>(row + 128) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    }
+    for (int rr = tid; rr < Co * 2; rr += 128) {  // B: weights of tap t, Co rows x 16 channels
+      const int co = rr >> 1, kc = rr & 1;
+      const __nv_bfloat16 *wp = w + ((size_t)co * Ci + ci0 + kc * 8) * K3 + t;
+      uint32_t pk[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) pk[j] = bf16_pair(wp[(size_t)(2 * j) * K3], wp[(size_t)(2 * j + 1) * K3]);
+      *reinterpret_cast<uint4 *>(sB[st] + (co >> 3) * 256 + kc * 128 + (co & 7) * 16) =
+          make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+    gt::fence_async_shared();
+    __syncthreads();
+    if (tid == 0) {
+      gt::tc_fence_after();
+      gt::tc_mma_bf16(tmem, gt::tc_smem_desc(sA[st], 128, 256), gt::tc_smem_desc(sB[st], 128, 256), idesc, q > 0);
+      gt::tc_commit(&bar[st]);
+    }
+    issued = q + 1;
+  }
+  // the last issued MMA's commit covers every earlier one
+  if (issued > 0) {
+    const int ql = issued - 1;
+    const bool done = gt::mbar_wait_bounded(&bar[ql & 1], (ql >> 1) & 1, TC_WAIT_LIMIT);
+    ok = ok && done;
+  }
+  ok = !__syncthreads_or(!ok);
+  gt::tc_fence_after();
+  if (ok) {
+    for (int c0 = 0; c0 < Co; c0 += 16) {
+      float v[16];
+      gt::tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (active) {
+        TO *yo = y + ((size_t)b * Cy + co_off + c0) * vol + (size_t)d * plane + (size_t)h * s.W + wx;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          float r = v[k] + (bias ? bias[c0 + k] : 0.f);
+          if (accumulate) r += ld<TO>(yo + (size_t)k * vol);
+          if (relu) r = fmaxf(r, 0.f);
+          st<TO>(yo + (size_t)k * vol, r);
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(&g_nn_err, 1);
+  }
+  gt::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) gt::tmem_dealloc(tmem, ncols);
+}
+
+int g_tc_mode = 1;  // 1: tensor-core path where it applies, 0: CUDA cores only
 
 // w[co][ci][t] -> w'[ci][co][K3-1-t]: convolving dY with w' gives dX (stride 1, same padding)
 __global__ void k_flip(const __nv_bfloat16 *__restrict__ w, __nv_bfloat16 *__restrict__ wf, int Co, int Ci, int K3) {
@@ -402,6 +540,20 @@ int gt_nn_conv3d(const void *x, int x_dtype, int Ci, int Cx, int x_off, const vo
   const Shape s{B, D, H, W};
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;
+  if (g_tc_mode && x_dtype == 1 && Ci % 16 == 0 && Co % 16 == 0 && Co <= 256) {
+    const unsigned g = (unsigned)(((long long)B * D * H * W + 127) / 128);
+    const __nv_bfloat16 *xb = (const __nv_bfloat16 *)x, *wb = (const __nv_bfloat16 *)w_bf16;
+    if (ksize == 3 && y_dtype == 1)
+      k_conv3d_tc<__nv_bfloat16, 3><<<g, 128, 0, st>>>(xb, Ci, Cx, x_off, wb, bias, (__nv_bfloat16 *)y, Co, Cy, co_off, s, relu, accumulate);
+    else if (ksize == 3)
+      k_conv3d_tc<float, 3><<<g, 128, 0, st>>>(xb, Ci, Cx, x_off, wb, bias, (float *)y, Co, Cy, co_off, s, relu, accumulate);
+    else if (y_dtype == 1)
+      k_conv3d_tc<__nv_bfloat16, 1><<<g, 128, 0, st>>>(xb, Ci, Cx, x_off, wb, bias, (__nv_bfloat16 *)y, Co, Cy, co_off, s, relu, accumulate);
+    else
+      k_conv3d_tc<float, 1><<<g, 128, 0, st>>>(xb, Ci, Cx, x_off, wb, bias, (float *)y, Co, Cy, co_off, s, relu, accumulate);
+    NN_CK(cudaGetLastError(), "gt_nn_conv3d (tensor cores)");
+    return GT_OK;
+  }
   if (x_dtype == 1 && y_dtype == 1)
     e = conv_k<__nv_bfloat16, __nv_bfloat16>(ksize, x, Ci, Cx, x_off, w_bf16, bias, y, Co, Cy, co_off, s, relu, accumulate, st);
   else if (x_dtype == 1 && y_dtype == 0)
@@ -413,6 +565,22 @@ int gt_nn_conv3d(const void *x, int x_dtype, int Ci, int Cx, int x_off, const vo
   else
     return gt::set_error(GT_ERR_ARG, "gt_nn_conv3d: dtype must be 0 (f32) or 1 (bf16)");
   NN_CK(e, "gt_nn_conv3d");
+  return GT_OK;
+}
+
+int gt_nn_set_tensor_cores(int on) {
+  g_tc_mode = on ? 1 : 0;
+  return GT_OK;
+}
+
+int gt_nn_check(void) {
+  int flag = 0;
+  NN_CK(cudaMemcpyFromSymbol(&flag, g_nn_err, sizeof(int)), "gt_nn_check");
+  if (flag) {
+    const int zero = 0;
+    NN_CK(cudaMemcpyToSymbol(g_nn_err, &zero, sizeof(int)), "gt_nn_check");
+    return gt::set_error(GT_ERR_TIMEOUT, "a tensor-core convolution block gave up waiting for its MMA");
+  }
   return GT_OK;
 }
 

@@ -230,7 +230,14 @@ GT_API int gt_batch_set_active(gt_batch *b, int k, int active);
  *   (ceil(n/256) floats in part).
  * gt_nn_adam: Adam step (bias-corrected, step >= 1) on float32 master weights,
  *   refreshing the bfloat16 copy when w_bf16 is not NULL.
- * gt_nn_cast: float32 <-> bfloat16 (src_dtype 0: f32 -> bf16, 1: bf16 -> f32). */
+ * gt_nn_cast: float32 <-> bfloat16 (src_dtype 0: f32 -> bf16, 1: bf16 -> f32).
+ * gt_nn_set_tensor_cores: 1 (default) runs gt_nn_conv3d with bfloat16 input,
+ *   Ci % 16 == 0, Co % 16 == 0 and Co <= 256 on the tensor cores (tcgen05 MMA, FP32
+ *   accumulator in tensor memory), 0 keeps every convolution on the CUDA cores.
+ * gt_nn_check: GT_ERR_TIMEOUT if a tensor-core convolution block gave up a bounded
+ *   wait since the last call (its output is then not written; the flag is cleared). */
+GT_API int gt_nn_set_tensor_cores(int on);
+GT_API int gt_nn_check(void);
 GT_API int gt_nn_conv3d(const void *x, int x_dtype, int Ci, int Cx, int x_off, const void *w_bf16, const float *bias,
                         void *y, int y_dtype, int Co, int Cy, int co_off, int B, int D, int H, int W, int ksize,
                         int relu, int accumulate, void *stream);

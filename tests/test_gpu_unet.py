@@ -254,7 +254,63 @@ def _ref_net(net, x, emulate):
     return out + base, params
 
 
-def test_unet_forward_backward_vs_float64():
+@pytest.mark.parametrize("tc", [0, 1])
+def test_unet_forward_backward_vs_float64(tc):
+    """tc = 0: every convolution on the CUDA cores, checked against a float64 network
+    that rounds the same activations to bfloat16 (tight) and against the unrounded
+    float64 network (loose).  tc = 1: the convolutions with 16k channels on the
+    tensor cores; their FP32 sums run in another order, so some bfloat16 roundings
+    of activations (and ReLU masks at zero) land on the other side of the
+    emulation's -- checked against the unrounded network only, with the same bound."""
+    L = _lib()
+    L.check(L.lib().gt_nn_set_tensor_cores(tc))
+    try:
+        _unet_forward_backward_vs_float64(tc)
+    finally:
+        L.check(L.lib().gt_nn_set_tensor_cores(1))
+
+
+def _unet_run(tc):
+    """Output and gradient of the test network on its fixed batch."""
+    from graptor_gb300.warmstart import UNet3D
+    L = _lib()
+    L.check(L.lib().gt_nn_set_tensor_cores(tc))
+    g = torch.Generator().manual_seed(2024)
+    cin, cout, B, D, H, W = 2, 8, 2, 8, 16, 16
+    net = UNet3D(cin, cout, residual=cin, seed=1)
+    o, ob, *_ = net.offsets["head"]
+    net.master[o:ob] = (torch.randn(ob - o, generator=g) * 0.25).cuda()
+    net.refresh()
+    x = (torch.rand((B, cin, D, H, W), generator=g) * 2).to(torch.bfloat16)
+    out = torch.empty((B, cout, D, H, W), device="cuda")
+    net.residual_base(x.cuda(), out)
+    net.forward(x.cuda(), out)
+    G = torch.randn((B, cout, D, H, W), generator=g)
+    net.backward(x.cuda(), G.cuda())
+    torch.cuda.synchronize()
+    L.check(L.lib().gt_nn_check())
+    return net, out.cpu(), net.grad.cpu()
+
+
+def test_unet_tensor_cores_agree_with_cuda_cores():
+    """The whole network with its 16k-channel convolutions on the tensor cores
+    against the same network on the CUDA cores: outputs within bfloat16 rounding;
+    weight and bias gradients within 15 %, the scale at which either bfloat16
+    network's gradients differ from the unrounded float64 network's (5-11 %:
+    activations rounded to bfloat16, ReLU masks at zero)."""
+    try:
+        net, out1, g1 = _unet_run(1)
+        _, out0, g0 = _unet_run(0)
+    finally:
+        _lib().check(_lib().lib().gt_nn_set_tensor_cores(1))
+    assert rel(out1, out0) < 5e-3
+    for name, ci, co, k in net.layers:
+        o, ob, *_ = net.offsets[name]
+        assert rel(g1[o:ob], g0[o:ob]) < 1.5e-1, name
+        assert rel(g1[ob:ob + co], g0[ob:ob + co]) < 1.5e-1, name
+
+
+def _unet_forward_backward_vs_float64(tc):
     from graptor_gb300.warmstart import UNet3D
     g = torch.Generator().manual_seed(2024)
     cin, cout, B, D, H, W = 2, 8, 2, 8, 16, 16
@@ -273,7 +329,8 @@ def test_unet_forward_backward_vs_float64():
     torch.cuda.synchronize()
     got_out, got_grad = out.cpu(), net.grad.cpu()
     report = {}
-    for emulate, tol_out, tol_grad in ((True, 1e-3, 5e-3), (False, 5e-2, 3e-1)):
+    cases = ((False, 5e-2, 3e-1),) if tc else ((True, 1e-3, 5e-3), (False, 5e-2, 3e-1))
+    for emulate, tol_out, tol_grad in cases:
         ref, params = _ref_net(net, x.double(), emulate)
         names = [n for n, *_ in net.layers]
         leaves = [t for n in names for t in params[n]]
@@ -304,3 +361,42 @@ def test_unet_overfits_one_batch():
     losses = [float(net.train_step(x, tgt, lr=3e-3)) for _ in range(300)]
     assert np.isfinite(losses).all()
     assert losses[-1] < 0.1 * losses[0], (losses[0], losses[-1])
+
+
+@pytest.mark.parametrize("k,Ci,Co,ydt", [(3, 16, 16, 0), (3, 32, 64, 1), (1, 48, 32, 0), (3, 16, 48, 0)])
+def test_conv_tensor_cores_match_cuda_cores(k, Ci, Co, ydt):
+    """The tcgen05 implicit-GEMM convolution (bfloat16 operands, FP32 accumulator in
+    tensor memory) against the CUDA-core kernel on the same bfloat16 inputs, with
+    channel views, bias, accumulation and ReLU; and against float64."""
+    L = _lib()
+    lib = L.lib()
+    g = torch.Generator().manual_seed(100 + k + Ci + Co)
+    B, D, H, W = 2, 5, 6, 12  # 720 voxels: five full 128-voxel tiles and a partial one
+    Cx, xoff, Cy, yoff = Ci + 16, 16, Co + 3, 2
+    x = _bf16((B, Cx, D, H, W), g)
+    w = _bf16((Co, Ci, k, k, k), g, 0.1)
+    bias = torch.randn(Co, generator=g)
+    ytype = torch.bfloat16 if ydt else torch.float32
+    y0 = torch.randn((B, Cy, D, H, W), generator=g).to(ytype)
+    outs = []
+    try:
+        for tc in (0, 1):
+            L.check(lib.gt_nn_set_tensor_cores(tc))
+            y = _d(y0)
+            xd, wd, bd = _d(x), _d(w), _d(bias)
+            L.check(lib.gt_nn_conv3d(_p(xd), 1, Ci, Cx, xoff, _p(wd), _p(bd), _p(y), ydt, Co, Cy, yoff, B, D, H, W, k,
+                                     1, 1, None))
+            torch.cuda.synchronize()
+            L.check(lib.gt_nn_check())
+            outs.append(y.cpu().double())
+    finally:
+        L.check(lib.gt_nn_set_tensor_cores(1))
+    ref = F.conv3d(x[:, xoff:xoff + Ci].double(), w.double(), bias.double(), padding=k // 2)
+    ref = torch.relu(ref + y0[:, yoff:yoff + Co].double())
+    sl = slice(yoff, yoff + Co)
+    tol = 1e-2 if ydt else 1e-5
+    assert rel(outs[1][:, sl], outs[0][:, sl]) < tol
+    assert rel(outs[1][:, sl], ref) < (1e-2 if ydt else 1e-5)
+    # channels outside the view are untouched
+    assert torch.equal(outs[1][:, :yoff], y0[:, :yoff].double())
+    assert torch.equal(outs[1][:, yoff + Co:], y0[:, yoff + Co:].double())
