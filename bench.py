@@ -497,7 +497,7 @@ def run_unet(args, rank, world, local):
 
 def run_warmstart(args, rank, world, local):
     """Time to relative primal-dual gap <= tol on held-out seeded problems
-    (3-D TGV-KL, FROB, 2 channels, 128^2 x 32, 71 angles): the plain solver
+    (3-D TGV-KL, FROB, 2 channels, 128^2 x 32 unless --n / --nz, 71 angles): the plain solver
     cold-started, problems one after another, against the learned warm start
     (pre cold iterations, U-Net prediction of u, lambda from K u; at a check
     that finds a problem's gap infinite, u is lifted along the rays with data
@@ -619,6 +619,12 @@ def main():
     ap.add_argument("--quick", action="store_true",
                     help="only the device-timed region (no e2e, kernel timing or CPU baseline): profiler runs")
     args = ap.parse_args()
+    if args.workload == "warmstart":  # --n / --nz size the warm-start problems instead
+        if args.nz:
+            WARM["Nz"] = int(args.nz)
+        if args.n:
+            WARM["N"] = int(args.n)
+        args.nz = args.n = None
     if args.nz:
         W["Nz"] = int(args.nz)
     if args.n:
