@@ -34,9 +34,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 W = dict(N=256, Nz=60, C=4, nang=71, alpha=(4.0, 1.0), mu=[0.2, 5e-4, 4e-3, 5e-4], peaks=[1e4, 20.0, 20.0, 20.0],
-         stated_iterations=2500)
+         stated_iterations=2500, coupling="FROB")
 METRIC = "voxel-iter/s"
-WORKLOAD_NAME = "3D FROB3D TGV-KL {N}x{N}x{Nz}, 4 channels, {N} bins x {nang} angles"
+WORKLOAD_NAME = "3D {cpl}3D TGV-KL {N}x{N}x{Nz}, 4 channels, {N} bins x {nang} angles"
+COUPLING_METHOD = {"FROB": "Frobenius 3D Reconstruction", "UNCORR": "Uncorrelated 3D Reconstruction",
+                   "NUCL": "Nuclear 3D Reconstruction"}
 
 
 def peaks():
@@ -158,7 +160,7 @@ def cpu_baseline(seconds=15.0):
     ang = phantom.angles_deg(nang)
     ofs = O.radon_struct(ang, N, N)
     f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
-    s = O.Solver(3, N, Nz, C, N, ofs, f, W["alpha"], W["mu"], 100.0, O.KL, O.TGV, O.FROB)
+    s = O.Solver(3, N, Nz, C, N, ofs, f, W["alpha"], W["mu"], 100.0, O.KL, O.TGV, getattr(O, W["coupling"]))
     s.run(1)
     t0 = time.perf_counter()
     it = 0
@@ -215,7 +217,7 @@ def run_reference(args, rank, world):
 
     def solver(Nz):
         f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
-        return O.Solver(3, N, Nz, C, N, ofs, f, W["alpha"], W["mu"], 100.0, O.KL, O.TGV, O.FROB)
+        return O.Solver(3, N, Nz, C, N, ofs, f, W["alpha"], W["mu"], 100.0, O.KL, O.TGV, getattr(O, W["coupling"]))
 
     probe = solver(2)
     t0 = time.perf_counter()
@@ -235,7 +237,7 @@ def run_reference(args, rank, world):
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"], nang=W["nang"]), "sample_slices": Nz},
+            "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"], nang=W["nang"], cpl=W["coupling"]), "sample_slices": Nz},
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": os.cpu_count(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -255,7 +257,7 @@ def run_ours(args, rank, world, local):
     f = np.concatenate([np.transpose(s, (1, 0, 2)) for s in sino])  # [S, nang, nd]
     stream = torch.cuda.Stream()
     forced = args.fwd_shape is not None or args.bp_shape is not None or args.dual_shape is not None
-    prob = Problem(3, N, Nz, C, N, ang, W["alpha"], W["mu"], "KL", "TGV", "FROB", 1.0, None, local,
+    prob = Problem(3, N, Nz, C, N, ang, W["alpha"], W["mu"], "KL", "TGV", W["coupling"], 1.0, None, local,
                    stream.cuda_stream, autotune=not forced)
     prob.set_data(f)
     if forced:  # launch shapes given on the command line (profiler captures): no tuning launches
@@ -281,7 +283,7 @@ def run_ours(args, rank, world, local):
         prob.close()
         return {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-                "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"], nang=W["nang"]), "Nz": Nz, "quick": True}, "clocks": clocks}
+                "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"], nang=W["nang"], cpl=W["coupling"]), "Nz": Nz, "quick": True}, "clocks": clocks}
 
     # ---- per-kernel durations (CUDA events on the launching stream) for the roofline
     kms = prob.time_kernels(reps=5)
@@ -312,7 +314,7 @@ def run_ours(args, rank, world, local):
     barrier(world)
     t0 = time.perf_counter()
     u, s_out = r3.Reconstructionapproach3d(sino, ang, W["alpha"], np.array(W["mu"]), args.steps, local, [0, 0.1], 1,
-                                           "KL", "Frobenius 3D Reconstruction", "TGV", [0.0, 1.0, [0]])
+                                           "KL", COUPLING_METHOD[W["coupling"]], "TGV", [0.0, 1.0, [0]])
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     h2d = 4 * Sb
     d2h = 4 * V + 4 * Sb
@@ -325,8 +327,8 @@ def run_ours(args, rank, world, local):
     out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": it_ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantoms, Poisson noise)",
-           "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"], nang=W["nang"]), "voxel_channels": V, "sinogram_bins": Sb, "dim": 3, "N": N,
-                      "Nz": Nz, "C": C, "nang": nang, "coupling": "FROB", "discrepancy": "KL",
+           "config": {"workload": WORKLOAD_NAME.format(N=W["N"], Nz=W["Nz"], nang=W["nang"], cpl=W["coupling"]), "voxel_channels": V, "sinogram_bins": Sb, "dim": 3, "N": N,
+                      "Nz": Nz, "C": C, "nang": nang, "coupling": W["coupling"], "discrepancy": "KL",
                       "regularisation": "TGV", "stated_iterations": W["stated_iterations"],
                       "time_for_stated_iterations_s": it_ms * W["stated_iterations"] / 1e3,
                       "l2": f"inputs larger than L2 (solver state {V * 76 / 1e9:.1f} GB per replica)",
@@ -495,6 +497,54 @@ def run_unet(args, rank, world, local):
                          "frac": flops / (ms / 1e3) / 1e12 / peak, "peak_source": kind, "traffic": None}}
 
 
+def run_subsample(args, rank, world, local):
+    """The two-resolution solver (radon_tgv_primal_dual_3dsubsample.py): channel 0 measured
+    on the fine grid (N bins x Nz slices), channel 1 on a grid twice as coarse (N/2 bins x
+    Nz/2 slices, pixel ratio 2, 2x2 binning of its fine projections), 71 angles each, TGV-KL
+    with Frobenius coupling of both channels on the fine grid.  value = fine-grid
+    voxel-channel iterations per second."""
+    import torch
+
+    from graptor_gb300 import _lib as L
+    from graptor_gb300 import phantom, solver
+    from graptor_gb300.radon_tgv_primal_dual_3dsubsample import Subsampling
+    torch.cuda.set_device(local)
+    N, Nz, nang = W["N"], W["Nz"], W["nang"]
+    if N % 2 or Nz % 2:
+        raise ValueError("the two-resolution workload needs even N and Nz")
+    vol = phantom.ellipsoids_3d(N, Nz, 2, 12, seed=rank)  # [c, z, y, x]
+    ang = phantom.angles_deg(nang)
+    img = torch.from_numpy(vol.reshape(2 * Nz, N * N).T.copy()).cuda()
+    sino = torch.zeros(nang * N, 2 * Nz, device="cuda")
+    solver.radon(img.data_ptr(), sino.data_ptr(), ang, N, N, 2 * Nz)
+    g = sino.cpu().numpy().T.reshape(2, Nz, nang, N)
+    f0 = phantom.poisson(g[0], 1e4, rank)                                  # [Nz, nang, N]
+    fine1 = phantom.poisson(g[1], 20.0, rank + 1)
+    f1 = 0.25 * (fine1[0::2, :, 0::2] + fine1[1::2, :, 0::2] + fine1[0::2, :, 1::2] + fine1[1::2, :, 1::2])
+    refnew, refold = [(N - 1) / 2.0, (Nz - 1) / 2.0], [(N / 2 - 1) / 2.0, (Nz / 2 - 1) / 2.0]
+    with Subsampling(N, Nz, 1, 1, N // 2, Nz // 2, ang, ang, W["alpha"], [0.2, 4e-3], 2.0, refold, refnew,
+                     device=local) as s:
+        s.set_data(f0, f1)
+        p = L.lib().gt_subs_problem(s._h)
+        s.run(args.warmup)
+        L.check(L.lib().gt_synchronize(p))
+        barrier(world)
+        t0 = time.perf_counter()
+        s.run(args.steps)
+        L.check(L.lib().gt_synchronize(p))
+        dt = max_over_ranks(time.perf_counter() - t0, world)
+    V = N * N * Nz * 2
+    if rank != 0:
+        return None
+    return {"metric": METRIC, "value": world * V * args.steps / dt, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 2-channel ellipsoid phantoms, Poisson peaks 1e4 / 20)",
+            "config": {"workload": f"two-resolution TGV-KL FROB: channel 0 {N}x{N}x{Nz} ({N} bins), channel 1 "
+                                   f"{N // 2} bins x {Nz // 2} slices (pixel ratio 2), {nang} angles each",
+                       "voxel_channels_fine_grid": V}}
+
+
 def run_warmstart(args, rank, world, local):
     """Time to relative primal-dual gap <= tol on held-out seeded problems
     (3-D TGV-KL, FROB, 2 channels, 128^2 x 32 unless --n / --nz, 71 angles): the plain solver
@@ -606,12 +656,14 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="image side (default 256); profiler captures")
     ap.add_argument("--nang", type=int, default=None,
                     help="projection angles (default 71; the 768^2 x 384 large run uses 141)")
-    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart", "unet"],
+    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart", "unet", "subsample"],
                     help="coupled3d: the 3-D 4-channel workload (default); batched: 64 uneven problems; "
                          "warmstart: time to gap, cold start against learned warm start + batch")
     ap.add_argument("--batch", type=int, default=64, help="problems per rank for --workload batched")
     ap.add_argument("--seeds", type=int, default=8, help="held-out problems per rank for --workload warmstart")
     ap.add_argument("--weights", default=None, help="network weights for --workload warmstart")
+    ap.add_argument("--coupling", default="FROB", choices=["FROB", "UNCORR", "NUCL"],
+                    help="channel coupling of the coupled3d workload (default FROB, the headline)")
     ap.add_argument("--fwd-shape", type=int, default=None,
                     help="force the forward projector's launch shape (no autotuning); profiler captures")
     ap.add_argument("--bp-shape", type=int, default=None, help="force the back projector's launch shape")
@@ -629,6 +681,7 @@ def main():
         W["Nz"] = int(args.nz)
     if args.n:
         W["N"] = int(args.n)
+    W["coupling"] = args.coupling
     if args.nang:
         W["nang"] = int(args.nang)
     rank, world, local = dist_setup(args.gpus)
@@ -640,6 +693,8 @@ def main():
         out = run_warmstart(args, rank, world, local)
     elif args.workload == "unet":
         out = run_unet(args, rank, world, local)
+    elif args.workload == "subsample":
+        out = run_subsample(args, rank, world, local)
     else:
         from oracle import oracle as O
         O.build()  # the CPU-baseline leg needs the oracle library (built before any GPU work)
