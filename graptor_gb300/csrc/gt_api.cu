@@ -275,8 +275,11 @@ int autotune(gt_problem *p) {
   // back-projection shapes 14 and 15 (TMA-staged sinogram rows) are bit-identical
   // but slower on every measured workload (256^2 x 60 x 4: 0.43 / 0.45 against
   // 0.36 ms); they stay selectable by gt_set_tuning and are not tuned
-  const int nc[3] = {gt::num_proj_configs(p->d.S, 0), std::min(14, gt::num_proj_configs(p->d.S, 1)),
-                     gt::num_dual_configs(p->P)};
+  constexpr int kMaxCfg = 32;
+  const int nc[3] = {std::min(kMaxCfg, gt::num_proj_configs(p->d.S, 0)),
+                     std::min(kMaxCfg, gt::num_proj_configs(p->d.S, 1)),
+                     std::min(kMaxCfg, gt::num_dual_configs(p->P))};
+  auto skipped = [](int which, int c) { return which == 1 && (c == 14 || c == 15); };
   p->P.fwd_cfg = 0;
   p->P.bp_cfg = 0;
   p->P.dual_cfg = 0;
@@ -294,7 +297,7 @@ int autotune(gt_problem *p) {
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   // configurations interleaved over several rounds; each keeps its fastest round
-  float ms_cfg[3][16];
+  float ms_cfg[3][kMaxCfg];
   for (auto &r : ms_cfg) for (float &v : r) v = 1e30f;
   int rc = GT_OK;
   const bool log = std::getenv("GRAPTOR_TUNE_LOG") != nullptr;
@@ -304,6 +307,7 @@ int autotune(gt_problem *p) {
       float best_ms = 1e30f;
       for (int c = 0; c < nc[which]; ++c) best_ms = std::min(best_ms, ms_cfg[which][c]);
       for (int c = 0; c < nc[which] && rc == GT_OK; ++c) {
+        if (skipped(which, c)) continue;
         // after the first round only configurations within 30 % of the best are timed again
         if (round > 0 && ms_cfg[which][c] > 1.3f * best_ms) continue;
         gt::IterParams Q = p->P;

@@ -1406,7 +1406,7 @@ __global__ void __launch_bounds__(256, MINB) k_fwd(const IterParams P) {
 // back projection: kernel `radon_ad` (3-D :818-844): linear interpolation
 // between detector bins floor(t) and floor(t)+1 at t = dot((x, y, 1, 0), ofs[j]).
 // ===========================================================================
-template <int VW, bool EXACT = true, int AU = 1, class SL = Slices<VW>>
+template <int VW, bool EXACT = true, int AU = 1, class SL = Slices<VW>, int UA = 2>
 __device__ __forceinline__ void radon_ad_pixel(const float *__restrict__ lam, size_t S, int nd, int nang,
                                                const float4 *__restrict__ ofs, float xf, float yf,
                                                const SL &sl, float (&acc)[VW]) {
@@ -1417,7 +1417,7 @@ __device__ __forceinline__ void radon_ad_pixel(const float *__restrict__ lam, si
   if constexpr (AU == 1) {
     // one angle at a time, taps accumulated as they arrive (the compiler overlaps
     // consecutive angles)
-#pragma unroll 2
+#pragma unroll UA
     for (; j < nang; ++j) {
       const float4 o = __ldg(ofs + j);
       const float tt = __fadd_rn(__fadd_rn(__fmul_rn(xf, o.x), __fmul_rn(yf, o.y)), o.z);
@@ -1748,7 +1748,7 @@ __global__ void __launch_bounds__(256) k_bp_run(const IterParams P) {
 
 // k_bp: back projection K* lambda of every (pixel, slice) into P.kstar; it only
 // needs lambda, so it runs beside k_dual.
-template <int VW, int AU, bool TAB, bool WL = false>
+template <int VW, int AU, bool TAB, bool WL = false, int UA = 2>
 __global__ void __launch_bounds__(256) k_bp(const IterParams P) {
   const Dims d = P.d;
   long long unit;
@@ -1765,7 +1765,7 @@ __global__ void __launch_bounds__(256) k_bp(const IterParams P) {
     radon_ad_table<VW, false, AU>(P.lam, d.S, d.nd, d.nang, P.bp_tab + (size_t)pix * d.nang, sl, acc);
   } else {
     const int y = pix / d.N, x = pix - y * d.N;
-    radon_ad_pixel<VW, false, AU>(P.lam, d.S, d.nd, d.nang, P.ofs, (float)x, (float)y, sl, acc);
+    radon_ad_pixel<VW, false, AU, decltype(sl), UA>(P.lam, d.S, d.nd, d.nang, P.ofs, (float)x, (float)y, sl, acc);
   }
   sl.store(P.kstar + (size_t)pix * d.S, acc);
 }
@@ -2806,7 +2806,7 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // which keeps all lanes busy when S is small.
 int num_proj_configs(int S, int which) {
   if (S % 4 != 0) return 1;
-  return which == 0 ? 17 : 16;  // configs 4 / 8 (one slice per thread) stay candidates for every S
+  return which == 0 ? 17 : 18;  // configs 4 / 8 (one slice per thread) stay candidates for every S
 }
 
 template <int VW, int UNR>
@@ -2887,6 +2887,11 @@ static void bp_vw(const IterParams &P, cudaStream_t st) {
   k_bp<VW, AU, TAB><<<blocks_for(threads_for<VW>((long long)P.d.N * P.d.N, P.d.S), 256), 256, 0, st>>>(P);
 }
 
+template <int UA>
+static void bp_ua(const IterParams &P, cudaStream_t st) {
+  k_bp<8, 1, false, false, UA><<<blocks_for(threads_for<8>((long long)P.d.N * P.d.N, P.d.S), 256), 256, 0, st>>>(P);
+}
+
 static void bp_wl(const IterParams &P, cudaStream_t st) {
   k_bp<1, 1, false, true><<<blocks_for(threads_for_wl((long long)P.d.N * P.d.N, P.d.S), 256), 256, 0, st>>>(P);
 }
@@ -2920,6 +2925,8 @@ cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
       case 15:
         if (P.bp_tmap_wide) bp_tma<8>(P, st); else bp_vw<8, 1, false>(P, st);
         break;
+      case 16: bp_ua<4>(P, st); break;  // the one-angle shape (4) with its angle loop unrolled 4x
+      case 17: bp_ua<1>(P, st); break;  // ... not unrolled (fewer instructions in flight, faster)
       default: bp_vw<8, 2>(P, st); break;
     }
   } else if (S % 2 == 0) {
