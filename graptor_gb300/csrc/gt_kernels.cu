@@ -2806,7 +2806,7 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // which keeps all lanes busy when S is small.
 int num_proj_configs(int S, int which) {
   if (S % 4 != 0) return 1;
-  return which == 0 ? 17 : 18;  // configs 4 / 8 (one slice per thread) stay candidates for every S
+  return which == 0 ? 20 : 18;  // configs 4 / 8 (one slice per thread) stay candidates for every S
 }
 
 template <int VW, int UNR>
@@ -2872,6 +2872,9 @@ cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
       case 14: fwd_vw_occ<8, 4, 4>(P, disc, st); break;
       case 15: fwd_vw_occ<8, 8, 4>(P, disc, st); break;
       case 16: fwd_vw_occ<4, 8, 4>(P, disc, st); break;
+      case 17: fwd_vw_occ<8, 2, 4>(P, disc, st); break;
+      case 18: fwd_vw_occ<8, 2, 5>(P, disc, st); break;
+      case 19: fwd_vw_occ<8, 4, 5>(P, disc, st); break;
       default: fwd_vw<8, 4>(P, disc, st); break;
     }
   } else if (S % 2 == 0) {

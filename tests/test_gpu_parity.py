@@ -225,7 +225,7 @@ def test_projector_launch_shapes_give_identical_iterates(S_case):
         from graptor_gb300 import _lib as L
         nf = L.lib().gt_set_tuning(p._h, 99, 0)
         assert nf != 0  # out of range is refused
-        configs = [(fc, 0) for fc in range(17)] + [(0, bc) for bc in range(1, 18)] if (C * Nz) % 4 == 0 else [(0, 0)]
+        configs = [(fc, 0) for fc in range(20)] + [(0, bc) for bc in range(1, 18)] if (C * Nz) % 4 == 0 else [(0, 0)]
         for fc, bc in configs:
             p.set_data(f)
             try:
