@@ -19,6 +19,7 @@
 #include <climits>
 #include <type_traits>
 #include <math.h>
+#include <cmath>
 
 #include "gt_common.cuh"
 #include "gt_tma.cuh"
@@ -3078,16 +3079,28 @@ cudaError_t fill_f32(float *x, size_t n, float v, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// power iteration: 30 rounds of  s = sum(img); img /= s; img = R^T R img  from the
-// all-ones image; returns sqrt(s) (the reference's 10 rounds from randn, in FP32).
+// power iteration: up to `rounds` rounds of  s = sum(img); img /= s; img = R^T R img
+// from the all-ones image, stopping once two consecutive sums agree to 1e-10;
+// returns sqrt(s) (the reference's 10 rounds from randn, in FP32).
 cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, double *d_img, double *d_sino,
                       double *d_part, double *out, cudaStream_t st) {
   const size_t n = (size_t)N * N;
   const int nb = 64;
   cudaError_t e;
+  double prev = 0.0;
   for (int r = 0; r < rounds; ++r) {
     k_sum64_partial<<<nb, 256, 0, st>>>(d_img, n, d_part);
     k_sum64_partial<<<1, 256, 0, st>>>(d_part, nb, d_part + nb);
+    if (r >= 4) {  // converged (consecutive estimates within 1e-10): stop early
+      double s = 0.0;
+      if ((e = cudaMemcpyAsync(&s, d_part + nb, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+      if (std::fabs(s - prev) <= 1e-10 * std::fabs(s)) {
+        *out = sqrt(s);
+        return cudaSuccess;
+      }
+      prev = s;
+    }
     k_scale64<<<64, 256, 0, st>>>(d_img, n, d_part + nb);
     k_radon64_warp<<<blocks_for(32LL * nd * nang, 256), 256, 0, st>>>(d_img, d_sino, ofs, N, nd, nang);
     k_radon_ad64<<<blocks_for((long long)n, 128), 128, 0, st>>>(d_sino, d_img, ofs, N, nd, nang);
