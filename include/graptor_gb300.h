@@ -235,7 +235,8 @@ GT_API int gt_batch_set_active(gt_batch *b, int k, int active);
  *   Ci % 16 == 0, Co % 16 == 0 and Co <= 256 on the tensor cores (tcgen05 MMA, FP32
  *   accumulator in tensor memory), 0 keeps every convolution on the CUDA cores.
  * gt_nn_check: GT_ERR_TIMEOUT if a tensor-core convolution block gave up a bounded
- *   wait since the last call (its output is then not written; the flag is cleared). */
+ *   wait since the last call (its output is then not written; the flag is cleared);
+ *   call it after synchronising the stream the convolutions ran on. */
 GT_API int gt_nn_set_tensor_cores(int on);
 GT_API int gt_nn_check(void);
 GT_API int gt_nn_conv3d(const void *x, int x_dtype, int Ci, int Cx, int x_off, const void *w_bf16, const float *bias,
