@@ -644,6 +644,112 @@ def ncu_traffic(kernel):
     return None
 
 
+def badproj_lane_ops(nz, nx, radius, pairs):
+    """FP32 lane operations of gt_badproj_compare: per interior pixel and shift, one
+    subtraction and one minimum in each of the two directions."""
+    mz, mx = nz - 2 * radius, nx - 2 * radius
+    return pairs * mz * mx * (2 * radius + 1) ** 2 * 4
+
+
+def run_badproj(args, rank, world, local):
+    """Bad-projection detection (find_bad_ele.py Find_Bad_projections) on a stack of
+    nang projections x N slices x N detector columns, default search radius.  A step is
+    one whole detection of the device-resident stack (smoothing, weighted gradients,
+    shifted comparisons of neighbours one and two apart, pair sums); value =
+    projections examined per second.  e2e = the public call with the host stack
+    (upload, detection, errors back, ranking)."""
+    import torch
+
+    from graptor_gb300 import badproj
+    torch.cuda.set_device(local)
+    NA, Nz, Nx = W["nang"], W["N"], W["N"]
+    rng = np.random.default_rng(rank)
+    zz, xx = np.meshgrid(np.arange(Nz), np.arange(Nx), indexing="ij")
+    base = np.zeros((Nz, Nx))
+    for _ in range(12):
+        cz, cx, r = rng.uniform(0.2, 0.8) * Nz, rng.uniform(0.2, 0.8) * Nx, rng.uniform(0.04, 0.12) * Nx
+        base += rng.uniform(0.5, 2.0) * ((zz - cz) ** 2 + (xx - cx) ** 2 < r * r)
+    data = np.stack([np.roll(base, int(rng.integers(-3, 4)), axis=1) for _ in range(NA)])
+    data += 0.05 * rng.random(data.shape)
+    for k in rng.choice(NA, 4, replace=False):
+        data[k] = np.roll(data[k], Nz // 5, axis=0) + 0.8 * rng.random((Nz, Nx))
+    d = badproj.upload(data, local)
+    S, Wg = badproj.stages(d)
+    r1 = int(min(S.shape[1], S.shape[2]) / 10)
+    r2 = int(r1 * 1.5)
+    nz, nx = Wg.shape[1], Wg.shape[2]
+    for _ in range(args.warmup):
+        badproj.detect(d)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # 256 MB > L2, between steps
+    st = torch.cuda.current_stream()
+    step_ms, cmp_ms = [], []
+    barrier(world)
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e[0].record(st)
+            S, Wg = badproj.stages(d)
+            e[1].record(st)
+            badproj.pair_errors(Wg, 1, r1)
+            badproj.pair_errors(Wg, 2, r2)
+            e[2].record(st)
+            e[2].synchronize()
+            step_ms.append(e[0].elapsed_time(e[2]))
+            cmp_ms.append(e[1].elapsed_time(e[2]))
+    torch.cuda.synchronize()
+    ms = max_over_ranks(sum(step_ms), world)
+    clocks = clk.summary()
+    if rank != 0:
+        return None
+    value = world * NA * args.steps / (ms / 1e3)
+    # e2e: the public call with the host stack
+    badproj.find_bad_projections("stack", None, 0.1, data=data, device=local)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(3, min(args.steps, 10))
+    import contextlib
+    import io
+    for _ in range(e2e_steps):
+        with contextlib.redirect_stdout(io.StringIO()):
+            badproj.find_bad_projections("stack", None, 0.1, data=data, device=local)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    # roofline of the comparison kernel: FP32 issue (subtract + minimum per shift and direction)
+    ops = badproj_lane_ops(nz, nx, r1, NA - 1) + badproj_lane_ops(nz, nx, r2, NA - 2)
+    cmp = statistics.median(cmp_ms)
+    nominal = 152 * 128 * 2.07e9  # lanes x maximum SM clock
+    roof = {"bound": "fp32-issue", "kernel": "k_compare", "achieved": ops / (cmp / 1e3), "peak": nominal,
+            "unit": "lane-op/s", "frac": ops / (cmp / 1e3) / nominal, "peak_source": "nominal (152 SMs x 128 lanes x 2.07 GHz)",
+            "traffic": None, "algorithmic_ops_per_step": ops, "ms_per_step": cmp}
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import badproj as obad
+        t0 = time.perf_counter()
+        Sh, Wh = obad.stages(data[:8])
+        t_stage = (time.perf_counter() - t0) / 8
+        k = 3
+        t0 = time.perf_counter()
+        obad.pair_errors(Wh[:k + 1], 1, r1)
+        t1 = (time.perf_counter() - t0) / k
+        t0 = time.perf_counter()
+        obad.pair_errors(Wh[:k + 2], 2, r2)
+        t2 = (time.perf_counter() - t0) / k
+        est = t_stage * NA + t1 * (NA - 1) + t2 * (NA - 2)
+        cpu = {"value": NA / est, "unit": "projections/s", "cores": 1, "kind": "port",
+               "sample": f"oracle (NumPy) stages of 8 projections and {k} pairs at each offset, scaled to {NA} projections"}
+    return {"metric": "projections/s", "value": value, "unit": "projections/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (box sums f64)",
+            "data": "synthetic (seeded blobs, shifts, noise, 4 corrupted projections)",
+            "config": {"workload": f"bad-projection detection: {NA} projections x {Nz} slices x {Nx} detector columns, "
+                                   f"search radius {r1} / {r2}",
+                       "l2": "256 MB written between steps (L2 flushed)"},
+            "e2e": {"value": NA / e2e_s, "unit": "projections/s", "h2d_bytes_per_step": int(data.nbytes),
+                    "d2h_bytes_per_step": 8 * (2 * NA - 3)},
+            "gpu_launches": 6 * args.steps, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -656,7 +762,7 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="image side (default 256); profiler captures")
     ap.add_argument("--nang", type=int, default=None,
                     help="projection angles (default 71; the 768^2 x 384 large run uses 141)")
-    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart", "unet", "subsample"],
+    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart", "unet", "subsample", "badproj"],
                     help="coupled3d: the 3-D 4-channel workload (default); batched: 64 uneven problems; "
                          "warmstart: time to gap, cold start against learned warm start + batch")
     ap.add_argument("--batch", type=int, default=64, help="problems per rank for --workload batched")
@@ -695,6 +801,8 @@ def main():
         out = run_unet(args, rank, world, local)
     elif args.workload == "subsample":
         out = run_subsample(args, rank, world, local)
+    elif args.workload == "badproj":
+        out = run_badproj(args, rank, world, local)
     else:
         from oracle import oracle as O
         O.build()  # the CPU-baseline leg needs the oracle library (built before any GPU work)

@@ -115,6 +115,10 @@ _SIGS = {
     "gt_nn_cast": (ctypes.c_int, [_P, _I, _P, _LL, _P]),
     "gt_nn_set_tensor_cores": (ctypes.c_int, [_I]),
     "gt_nn_check": (ctypes.c_int, []),
+    "gt_badproj_smooth": (ctypes.c_int, [_P, _I, _I, _I, _I, _P, _P]),
+    "gt_badproj_wgrad": (ctypes.c_int, [_P, _I, _I, _I, _P, _P]),
+    "gt_badproj_blocks": (ctypes.c_int, [_I, _I, _I]),
+    "gt_badproj_compare": (ctypes.c_int, [_P, _I, _I, _I, _I, _I, _P, _P, _P, _P]),
     "gt_subs_create": (ctypes.c_int, [ctypes.POINTER(GtSubsDesc), ctypes.POINTER(ctypes.c_void_p)]),
     "gt_subs_destroy": (None, [_P]),
     "gt_subs_set_data": (ctypes.c_int, [_P, _P, _P, _I]),

@@ -125,13 +125,13 @@ def _save(result, channelnames, solution, sino):
         mrc.write_mrc(f"{result}_all_channels_normalized.mrc", coll)
 
 
-def _load(names, datahandling, badprojections, find_bad, scalepars, section, dims3):
+def _load(names, datahandling, badprojections, find_bad, scalepars, section, dims3, device=0):
     brightness, baseline, cutedges, badfile, threshold = datahandling[:5]
     cutedges, threshold = float(cutedges), float(threshold)
     bad = list(badprojections)
     if find_bad[0] not in (0, 0.0):
         from .badproj import find_bad_projections
-        bad.extend(find_bad_projections(names[0], find_bad[1], find_bad[0]))
+        bad.extend(find_bad_projections(names[0], find_bad[1], find_bad[0], device=device))
     data, ratio, noise, angles = [], [], [], None
     for n in names:
         d, angles, avg = preprocess.load_channel(n, brightness, badfile, cutedges, bad)
@@ -157,7 +157,7 @@ def reconstruct_2d(names, result, mu, alpha, maxiter, method, levels, datahandli
     from .radon_tgv_primal_dual_2d import Reconstructionapproach2d
     section = range(levels[0], levels[1] + 1, levels[2])
     data, ratio, noise, angles, baseline, threshold = _load(names, datahandling, badprojections, find_bad, scalepars,
-                                                            section, False)
+                                                            section, False, device)
     C = len(names)
     nang, _, Nx = data[0].shape
     Nz = len(section)
@@ -190,7 +190,7 @@ def reconstruct_3d(names, result, mu, alpha, maxiter, method, levels, datahandli
     from .radon_tgv_primal_dual_3d import Reconstructionapproach3d
     section = list(range(levels[0], levels[1] + 1, levels[2]))
     data, ratio, noise, angles, baseline, threshold = _load(names, datahandling, badprojections, find_bad, scalepars,
-                                                            section, True)
+                                                            section, True, device)
     C = len(names)
     coll = []
     for i in range(C):

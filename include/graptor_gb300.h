@@ -330,6 +330,30 @@ GT_API gt_problem *gt_subs_problem(gt_subs *s);
 /* Number of kernel launches one iteration issues (for launch accounting). */
 GT_API int gt_launches_per_iteration(const gt_problem *p);
 
+/* Detection of unsuitable projections: the array stages of Find_Bad_projections
+ * (find_bad_ele.py:139-230), whose host steps (loading, subsampling, combining the
+ * neighbour errors, ranking) stay with the caller.  Stacks are [na][nz][nx] with nx
+ * fastest; all pointers are device pointers; calls are asynchronous on `stream`.
+ *
+ * gt_badproj_smooth: out [na][nz-2s][nx-2s] (float32) = the (2s+1)^2 box sum of data
+ *   (float64, summed in float64 row by row) / (4 s^2)       (reduce_noise, :69-75; s >= 1)
+ * gt_badproj_wgrad: w [na][nz-2][nx-2] = max over the 8 neighbours of |c - nb|
+ *   (diagonals divided by sqrt 2) times min |nb|, in float32   (weighted_gradient, :103-136)
+ * gt_badproj_blocks: number of partial sums gt_badproj_compare writes per pair for this
+ *   image size and radius; 0 when the radius leaves no interior pixel.
+ * gt_badproj_compare: for every pair q = 0 .. na-offset-1 of projections (q, q+offset),
+ *   err[q] = sum over the interior [r, nz-r) x [r, nx-r) of
+ *   max(min_shift |U - V shifted|, min_shift |V - U shifted|), shifts |dz|, |dx| <= r,
+ *   differences in float32, sums in float64 (compare_shift_twosided, :55-100, with the
+ *   pairs of :177-190).  part holds gt_badproj_blocks(nz, nx, r) * (na - offset)
+ *   doubles; e_out, when not NULL, receives the per-pixel maxima [na-offset][nz-2r][nx-2r].
+ *   GT_ERR_ARG when the radius leaves no interior pixel. */
+GT_API int gt_badproj_smooth(const double *data, int na, int nz, int nx, int steps, float *out, void *stream);
+GT_API int gt_badproj_wgrad(const float *u, int na, int nz, int nx, float *w, void *stream);
+GT_API int gt_badproj_blocks(int nz, int nx, int radius);
+GT_API int gt_badproj_compare(const float *w, int na, int nz, int nx, int offset, int radius, double *part,
+                              double *err, float *e_out, void *stream);
+
 GT_API const char *gt_last_error(void);
 GT_API const char *gt_version(void);
 

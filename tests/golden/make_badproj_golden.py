@@ -11,6 +11,10 @@ is replaced by a function returning the seeded input stack -- ``mrcfile``,
 detector columns (the reference's subsampling branch does not run on Python 3)
 and an explicit search radius (its default, ``min(Nx, Nz)/10``, calls NumPy's ``min``
 through ``from numpy import *`` and raises).
+Besides the helpers' outputs on float64 and float32 arrays and the selections, it
+records every stage of ``Find_Bad_projections`` as the reference's helpers returned
+it inside the pipeline (smoothed stack, weighted gradients, the neighbour errors of
+projections one and two apart).
 Output: tests/golden/badproj.npz.
 """
 from __future__ import annotations
@@ -67,9 +71,37 @@ def main():
         nrm, E = fb.compare_shift_twosided(res[f"{n}/wgrad0"], w1, 4)
         res[f"{n}/shift_norm"] = np.array(nrm)
         res[f"{n}/shift_E"] = E
+        # the helpers on the float32 arrays Find_Bad_projections stores (:152-175)
+        w0f = fb.weighted_gradient(sm.astype(np.float32))[1]
+        res[f"{n}/wgrad0_f32"] = w0f
+        w1f = fb.weighted_gradient(fb.reduce_noise(data[1], 3).astype(np.float32))[1]
+        nrm, E = fb.compare_shift_twosided(w0f.astype(np.float32), w1f.astype(np.float32), 4)
+        res[f"{n}/shift_norm_f32"] = np.array(nrm)
+        res[f"{n}/shift_E_f32"] = E
         for frac in (0.15, 3):
             current["data"] = data
-            res[f"{n}/bad_{frac}"] = np.array(fb.Find_Bad_projections("stack", 4, frac))
+            rec = {"rn": [], "wg": [], "cmp": []}
+            helpers = (fb.reduce_noise, fb.weighted_gradient, fb.compare_shift_twosided)
+
+            def recorder(key, fn):
+                def call(*a):
+                    out = fn(*a)
+                    rec[key].append(out)
+                    return out
+                return call
+
+            fb.reduce_noise, fb.weighted_gradient, fb.compare_shift_twosided = (
+                recorder("rn", helpers[0]), recorder("wg", helpers[1]), recorder("cmp", helpers[2]))
+            try:
+                res[f"{n}/bad_{frac}"] = np.array(fb.Find_Bad_projections("stack", 4, frac))
+            finally:
+                fb.reduce_noise, fb.weighted_gradient, fb.compare_shift_twosided = helpers
+            if frac == 3:  # every stage of the pipeline, as the reference's helpers returned it
+                NA = data.shape[0]
+                res[f"{n}/pipe_smooth"] = np.stack(rec["rn"]).astype(np.float32)
+                res[f"{n}/pipe_wgrad"] = np.stack([w for _, w in rec["wg"]]).astype(np.float32)
+                norms = np.array([c[0] for c in rec["cmp"]])
+                res[f"{n}/pipe_err1"], res[f"{n}/pipe_err2"] = norms[:NA - 1], norms[NA - 1:]
     np.savez_compressed(os.path.join(HERE, "badproj.npz"), **res)
     print("wrote", os.path.join(HERE, "badproj.npz"), {k: v.shape for k, v in res.items() if "bad_" in k})
 

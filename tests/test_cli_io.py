@@ -1,6 +1,6 @@
 """CPU tests of the command-line path: MRC / angle-file I/O, preprocessing, the
-option handling of the reference CLI, and the bad-projection detector against
-golden vectors produced by the reference's own find_bad_ele.py
+option handling of the reference CLI, and the bad-projection detector's oracle and
+host steps against golden vectors produced by the reference's own find_bad_ele.py
 (tests/golden/make_badproj_golden.py)."""
 import os
 
@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from graptor_gb300 import badproj, cli, mrc, preprocess
+from oracle import badproj as obad
 
 
 def test_mrc_roundtrip_modes(tmp_path):
@@ -106,21 +107,50 @@ def test_cli_option_handling(tmp_path):
         cli.main([p, "--SliceLevels", "3", "1", "--Outfile", str(tmp_path / "o")])
 
 
-def test_bad_projections_match_reference(golden):
+def test_bad_projection_oracle_matches_reference(golden):
+    """The detector's oracle against the reference's own helpers and pipeline: the
+    helpers on float64 and on float32 arrays, every stage of Find_Bad_projections
+    (smoothed stack, weighted gradients, neighbour errors) and the selections, all
+    bit-exact."""
     g = golden("badproj.npz")
     for n in sorted({k.split("/")[0] for k in g}):
         data = g[f"{n}/data"]
-        sm = badproj.reduce_noise(data[0], 3)
-        np.testing.assert_allclose(sm, g[f"{n}/reduce_noise0"], rtol=1e-13, atol=0)
-        w0 = badproj.weighted_gradient(sm)[1]
-        np.testing.assert_allclose(w0, g[f"{n}/wgrad0"], rtol=1e-13, atol=0)
-        w1 = badproj.weighted_gradient(badproj.reduce_noise(data[1], 3))[1]
-        nrm, E = badproj.compare_shift_twosided(w0, w1, 4)
-        np.testing.assert_allclose(E, g[f"{n}/shift_E"], rtol=1e-13, atol=0)
-        assert np.isclose(nrm, float(g[f"{n}/shift_norm"]), rtol=1e-12)
+        sm = obad.reduce_noise(data[0], 3)
+        np.testing.assert_array_equal(sm, g[f"{n}/reduce_noise0"])
+        w0 = obad.weighted_gradient(sm)[1]
+        np.testing.assert_array_equal(w0, g[f"{n}/wgrad0"])
+        w1 = obad.weighted_gradient(obad.reduce_noise(data[1], 3))[1]
+        nrm, E = obad.compare_shift_twosided(w0, w1, 4)
+        np.testing.assert_array_equal(E, g[f"{n}/shift_E"])
+        assert nrm == float(g[f"{n}/shift_norm"])
+        # float32, as the detector stores its stacks
+        w0f = obad.weighted_gradient(sm.astype(np.float32))[1]
+        np.testing.assert_array_equal(w0f, g[f"{n}/wgrad0_f32"])
+        w1f = obad.weighted_gradient(obad.reduce_noise(data[1], 3).astype(np.float32))[1]
+        nrm, E = obad.compare_shift_twosided(w0f.astype(np.float32), w1f.astype(np.float32), 4)
+        np.testing.assert_array_equal(E, g[f"{n}/shift_E_f32"])
+        assert nrm == float(g[f"{n}/shift_norm_f32"])
+        S, W = obad.stages(data)
+        np.testing.assert_array_equal(S, g[f"{n}/pipe_smooth"])
+        np.testing.assert_array_equal(W, g[f"{n}/pipe_wgrad"])
+        assert obad.pair_errors(W, 1, 4) == list(g[f"{n}/pipe_err1"])
+        assert obad.pair_errors(W, 2, 6) == list(g[f"{n}/pipe_err2"])
         for frac in ("0.15", "3"):
-            got = badproj.find_bad_projections("stack", 4, float(frac) if "." in frac else int(frac), data=data)
+            got = obad.find_bad_projections(data, 4, float(frac) if "." in frac else int(frac))
             assert list(got) == list(g[f"{n}/bad_{frac}"]), (n, frac)
+
+
+def test_bad_projection_host_selection_matches_oracle():
+    """The product's host step (combining neighbour errors and ranking) is the
+    oracle's, including count-style fractions, -1 and ties (first index wins)."""
+    rng = np.random.default_rng(5)
+    for NA in (3, 4, 9, 30):
+        e1 = list(rng.random(NA - 1))
+        e2 = list(rng.random(NA - 2))
+        for frac in (0.1, 0.5, -1, 2, 1):
+            assert badproj.select(e1, e2, frac) == obad.select(e1, e2, frac)
+    tie = [1.0, 1.0, 1.0, 1.0]
+    assert badproj.select(tie, tie[:3], 3)[0] == obad.select(tie, tie[:3], 3)[0] == [1, 2, 3]
 
 
 def test_subsampling_geometry_helpers():
