@@ -13,8 +13,8 @@
 //                       :55-100, called at :177-190)
 //
 // The comparison dominates (radius^2 work per pixel).  A block covers 32 columns x
-// 32 rows of one pair; a thread owns one column and four consecutive rows, so every
-// value loaded from the shifted window serves up to four pixels (a sliding column
+// 32 rows of one pair; a thread owns one column and eight consecutive rows, so every
+// value loaded from the shifted window serves up to eight pixels (a sliding column
 // window) and the loop is bound by FP32 issue, not by loads.  The per-pixel minima
 // are exact in FP32 (rounding is monotone, so the minimum of rounded differences is
 // the rounded minimum, which is what the reference's FP32 subtraction yields); the
@@ -27,8 +27,8 @@
 namespace {
 
 constexpr int CMP_TX = 32;          // columns per block (one warp wide)
-constexpr int CMP_TY = 8;           // warps per block
-constexpr int CMP_ROWS = 4;         // rows per thread
+constexpr int CMP_TY = 4;           // warps per block
+constexpr int CMP_ROWS = 8;         // rows per thread
 constexpr int CMP_TILE_Y = CMP_TY * CMP_ROWS;
 
 inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -77,20 +77,23 @@ __global__ void k_wgrad(const float *__restrict__ u, int na, int nz, int nx, flo
   w[i] = e * m;  // FP32 product = the FP64 product (exact) rounded to FP32
 }
 
-template <int J0, int J1>
+// the pixels j in [j0, j1] take the window values a (from V) and b (from U)
 __device__ __forceinline__ void cmp_upd(float (&m1)[CMP_ROWS], float (&m2)[CMP_ROWS], const float (&u)[CMP_ROWS],
-                                        const float (&v)[CMP_ROWS], float a, float b) {
+                                        const float (&v)[CMP_ROWS], float a, float b, int j0, int j1) {
 #pragma unroll
-  for (int j = J0; j <= J1; ++j) {
-    m1[j] = fminf(m1[j], fabsf(u[j] - a));
-    m2[j] = fminf(m2[j], fabsf(v[j] - b));
-  }
+  for (int j = 0; j < CMP_ROWS; ++j)
+    if (j >= j0 && j <= j1) {
+      m1[j] = fminf(m1[j], fabsf(u[j] - a));
+      m2[j] = fminf(m2[j], fabsf(v[j] - b));
+    }
 }
 
-// grid (tiles per pair, pairs), block (32, 8).  Pair q compares projection q (U)
+// grid (tiles per pair, pairs), block (32, 4).  Pair q compares projection q (U)
 // with q + offset (V) on the interior [r, nz - r) x [r, nx - r).  Column x of the
-// interior, rows y0 .. y0 + 3; row t of the sliding window is image row y0 + t,
-// t in [0, 2r + 3]; interior row y0 + j (image row y0 + j + r) uses t in [j, j + 2r].
+// interior, rows y0 .. y0 + 7; row t of the sliding window is image row y0 + t,
+// t in [0, 2r + 7]; interior row y0 + j (image row y0 + j + r) uses t in [j, j + 2r].
+// With 2r >= 7 the window splits into a head (t < 7: rows j <= t), a middle
+// (every row) and a tail (t > 2r: rows j >= t - 2r), all with compile-time row sets.
 __global__ void __launch_bounds__(CMP_TX *CMP_TY) k_compare(const float *__restrict__ W, int nz, int nx, int offset,
                                                             int r, int tiles_x, int tiles, double *__restrict__ part,
                                                             float *__restrict__ e_out) {
@@ -112,28 +115,29 @@ __global__ void __launch_bounds__(CMP_TX *CMP_TY) k_compare(const float *__restr
     m1[j] = __int_as_float(0x7f800000);
     m2[j] = __int_as_float(0x7f800000);
   }
-  // every window row in the image (all warps but the bottom edge's): no clamping
-  const bool fast = r >= 1 && y0 + 2 * r + CMP_ROWS - 1 <= nz - 1;
+  // every window row in the image (all warps but the bottom edge's) and the head
+  // and tail apart: no clamping, no run-time row tests
+  const bool fast = 2 * r >= CMP_ROWS - 1 && y0 + 2 * r + CMP_ROWS - 1 <= nz - 1;
   for (int l = -r; l <= r; ++l) {
     const float *pv = V + x + l;
     const float *pu = U + x + l;
     if (fast) {
       pv += (size_t)y0 * nx;
       pu += (size_t)y0 * nx;
-      cmp_upd<0, 0>(m1, m2, u, v, __ldg(pv), __ldg(pu));
-      cmp_upd<0, 1>(m1, m2, u, v, __ldg(pv + nx), __ldg(pu + nx));
-      cmp_upd<0, 2>(m1, m2, u, v, __ldg(pv + 2 * nx), __ldg(pu + 2 * nx));
-      pv += 3 * nx;
-      pu += 3 * nx;
-#pragma unroll 4
-      for (int t = 3; t <= 2 * r; ++t) {
-        cmp_upd<0, 3>(m1, m2, u, v, __ldg(pv), __ldg(pu));
+#pragma unroll
+      for (int t = 0; t < CMP_ROWS - 1; ++t)
+        cmp_upd(m1, m2, u, v, __ldg(pv + t * nx), __ldg(pu + t * nx), 0, t);
+      pv += (CMP_ROWS - 1) * nx;
+      pu += (CMP_ROWS - 1) * nx;
+#pragma unroll 2
+      for (int t = CMP_ROWS - 1; t <= 2 * r; ++t) {
+        cmp_upd(m1, m2, u, v, __ldg(pv), __ldg(pu), 0, CMP_ROWS - 1);
         pv += nx;
         pu += nx;
       }
-      cmp_upd<1, 3>(m1, m2, u, v, __ldg(pv), __ldg(pu));
-      cmp_upd<2, 3>(m1, m2, u, v, __ldg(pv + nx), __ldg(pu + nx));
-      cmp_upd<3, 3>(m1, m2, u, v, __ldg(pv + 2 * nx), __ldg(pu + 2 * nx));
+#pragma unroll
+      for (int t = 1; t < CMP_ROWS; ++t)
+        cmp_upd(m1, m2, u, v, __ldg(pv + (t - 1) * nx), __ldg(pu + (t - 1) * nx), t, CMP_ROWS - 1);
     } else {
       for (int t = 0; t <= 2 * r + CMP_ROWS - 1; ++t) {
         const size_t row = (size_t)min(y0 + t, nz - 1);  // rows past the image serve only rows past the interior
