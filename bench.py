@@ -764,7 +764,9 @@ def main():
                     help="projection angles (default 71; the 768^2 x 384 large run uses 141)")
     ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart", "unet", "subsample", "badproj"],
                     help="coupled3d: the 3-D 4-channel workload (default); batched: 64 uneven problems; "
-                         "warmstart: time to gap, cold start against learned warm start + batch")
+                         "warmstart: time to gap, cold start against learned warm start + batch; unet: the "
+                         "warm-start network's forward pass; subsample: the two-resolution solver; badproj: "
+                         "bad-projection detection on nang projections x N x N")
     ap.add_argument("--batch", type=int, default=64, help="problems per rank for --workload batched")
     ap.add_argument("--seeds", type=int, default=8, help="held-out problems per rank for --workload warmstart")
     ap.add_argument("--weights", default=None, help="network weights for --workload warmstart")

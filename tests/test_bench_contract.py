@@ -37,3 +37,16 @@ def test_bench_cli_options():
     assert r.returncode == 0
     for opt in ("--gpus", "--steps", "--warmup", "--impl", "--workload", "--coupling", "--fwd-shape", "--quick"):
         assert opt in r.stdout, opt
+
+
+def test_badproj_work_count():
+    """The comparison kernel's algorithmic count (roofline numerator) against a
+    direct count of (pixel, shift, direction) triples times two operations."""
+    sys.path.insert(0, ROOT)
+    import bench
+    for nz, nx, r, pairs in ((20, 30, 3, 4), (9, 33, 4, 1), (40, 40, 0, 2)):
+        direct = 0
+        for y in range(r, nz - r):
+            for x in range(r, nx - r):
+                direct += sum(1 for k in range(-r, r + 1) for l in range(-r, r + 1)) * 2 * 2
+        assert bench.badproj_lane_ops(nz, nx, r, pairs) == pairs * direct
