@@ -64,6 +64,20 @@ def test_null_arguments():
     assert lib.gt_set_data(None, None, 1) == L.GT_ERR_ARG
     assert lib.gt_get_state(None, 0, None) == L.GT_ERR_ARG
     lib.gt_problem_destroy(None)
+    # bad-projection stages: rejected on the host before any launch
+    assert lib.gt_badproj_smooth(None, 3, 40, 40, 3, None, None) == L.GT_ERR_ARG
+    assert lib.gt_badproj_wgrad(None, 3, 40, 40, None, None) == L.GT_ERR_ARG
+    assert lib.gt_badproj_compare(None, 3, 40, 40, 1, 3, None, None, None, None) == L.GT_ERR_ARG
+
+
+def test_badproj_block_count():
+    """Partial sums per pair: 32 x 32 interior tiles; 0 when the radius leaves no interior."""
+    lib = L.lib()
+    assert lib.gt_badproj_blocks(20, 30, 3) == 1
+    assert lib.gt_badproj_blocks(100, 100, 2) == 9
+    assert lib.gt_badproj_blocks(248, 248, 25) == 7 * 7
+    assert lib.gt_badproj_blocks(20, 30, 10) == 0
+    assert lib.gt_badproj_blocks(20, 30, -1) == 0
 
 
 def test_error_mapping():
