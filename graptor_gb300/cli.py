@@ -125,13 +125,25 @@ def _save(result, channelnames, solution, sino):
         mrc.write_mrc(f"{result}_all_channels_normalized.mrc", coll)
 
 
-def _load(names, datahandling, badprojections, find_bad, scalepars, section, dims3, device=0):
+def _load(names, datahandling, badprojections, find_bad, scalepars, section, dims3, device=0, apply_found=False):
+    """Load, clean and scale every channel (2-D: :129-170; 3-D: :320-345).
+
+    The projections ``--Find_Bad_Projections`` finds are reported but, as in the
+    reference, not removed: it appends the list as one entry of ``Badprojections``
+    (:138, :328), and the loader's ``i+1 in text`` test (h5utilities.py:144-165)
+    never matches a list.  ``apply_found`` (``--Apply_Found_Projections``) removes
+    them."""
     brightness, baseline, cutedges, badfile, threshold = datahandling[:5]
     cutedges, threshold = float(cutedges), float(threshold)
     bad = list(badprojections)
     if find_bad[0] not in (0, 0.0):
         from .badproj import find_bad_projections
-        bad.extend(find_bad_projections(names[0], find_bad[1], find_bad[0], device=device))
+        found = find_bad_projections(names[0], find_bad[1], find_bad[0], device=device)
+        if apply_found:
+            bad.extend(found)
+        else:
+            eprint("Note: as in the reference, the projections found are not removed "
+                   "(--Apply_Found_Projections removes them).")
     data, ratio, noise, angles = [], [], [], None
     for n in names:
         d, angles, avg = preprocess.load_channel(n, brightness, badfile, cutedges, bad)
@@ -152,12 +164,12 @@ def _load(names, datahandling, badprojections, find_bad, scalepars, section, dim
 
 
 def reconstruct_2d(names, result, mu, alpha, maxiter, method, levels, datahandling, badprojections, find_bad,
-                   channelnames, regularisation, discrepancy, scalepars, device=0):
+                   channelnames, regularisation, discrepancy, scalepars, device=0, apply_found=False):
     """Slice-by-slice 2-D reconstruction (Coupled_Reconstruction2d)."""
     from .radon_tgv_primal_dual_2d import Reconstructionapproach2d
     section = range(levels[0], levels[1] + 1, levels[2])
     data, ratio, noise, angles, baseline, threshold = _load(names, datahandling, badprojections, find_bad, scalepars,
-                                                            section, False, device)
+                                                            section, False, device, apply_found)
     C = len(names)
     nang, _, Nx = data[0].shape
     Nz = len(section)
@@ -183,14 +195,15 @@ def reconstruct_2d(names, result, mu, alpha, maxiter, method, levels, datahandli
 
 
 def reconstruct_3d(names, result, mu, alpha, maxiter, method, levels, datahandling, badprojections, find_bad,
-                   channelnames, regularisation, discrepancy, overlay, chunksize, scalepars, device=0):
+                   channelnames, regularisation, discrepancy, overlay, chunksize, scalepars, device=0,
+                   apply_found=False):
     """Volumetric reconstruction in slice chunks with overlap (Coupled_Reconstruction3d):
     chunks of at most ``chunksize`` slices (all of them when <= 0), shrunk by 0.7 and
     retried when the device runs out of memory."""
     from .radon_tgv_primal_dual_3d import Reconstructionapproach3d
     section = list(range(levels[0], levels[1] + 1, levels[2]))
     data, ratio, noise, angles, baseline, threshold = _load(names, datahandling, badprojections, find_bad, scalepars,
-                                                            section, True, device)
+                                                            section, True, device, apply_found)
     C = len(names)
     coll = []
     for i in range(C):
@@ -443,6 +456,8 @@ def build_parser():
     p.add_argument("--Datahandling2", nargs="+", default=["bright", "thresholding", "0.0", "", "0.05"])
     p.add_argument("--Badprojections2", default=[], type=int, nargs="+")
     p.add_argument("--Find_Bad_Projections", nargs="+", default=[], type=float)
+    p.add_argument("--Apply_Found_Projections", action="store_true",
+                   help="remove the projections --Find_Bad_Projections finds (the reference reports them only)")
     p.add_argument("--Overlapping", default=1, type=int)
     p.add_argument("--Chunksize", default=-1, type=int)
     p.add_argument("--Scalepars", default=[1, 98], type=int, nargs="+")
@@ -513,10 +528,11 @@ def main(argv=None):
                              args.Overlapping, args.Chunksize, args.Scalepars, device)
     elif setting == 1:
         u = reconstruct_3d(names, args.Outfile, mu, alpha, args.Maxiter, method, levels, dh, args.Badprojections,
-                           find_bad, chn, reg, disc, args.Overlapping, args.Chunksize, args.Scalepars, device)
+                           find_bad, chn, reg, disc, args.Overlapping, args.Chunksize, args.Scalepars, device,
+                           args.Apply_Found_Projections)
     else:
         u = reconstruct_2d(names, args.Outfile, mu, alpha, args.Maxiter, method, levels, dh, args.Badprojections,
-                           find_bad, chn, reg, disc, args.Scalepars, device)
+                           find_bad, chn, reg, disc, args.Scalepars, device, args.Apply_Found_Projections)
     print("\nAlgorithm completed, results are written in " + outdir + ".")
     return u
 

@@ -90,6 +90,31 @@ def test_brightness_correction_and_rescaling(tmp_path):
     assert np.allclose(d2, d)
 
 
+def test_found_projections_reported_not_removed(tmp_path, monkeypatch):
+    """The reference appends the detector's list as one entry of Badprojections
+    (Reconstruction_coupled.py:138, :328); its loader's ``i+1 in text`` never matches
+    a list, so nothing found is removed.  The CLI does the same by default and
+    removes them with --Apply_Found_Projections.  The detector is a host fake here."""
+    rng = np.random.default_rng(4)
+    p = _stack(tmp_path, rng.random((6, 5, 20)) + 1.0, np.linspace(-60, 60, 6))
+    calls = []
+
+    def fake(name, searchradius, prozent, device=0):
+        calls.append((name, searchradius, prozent, device))
+        return [3, 6]
+
+    monkeypatch.setattr(badproj, "find_bad_projections", fake)
+    dh = ["bright", "thresholding", "0.0", "", "0.05"]
+    common = (dh, [1], [0.1, 2.0], [1, 98], range(0, 5), True)
+    kept = cli._load([p], *common, device=0)
+    assert calls == [(p, 2.0, 0.1, 0)]
+    assert kept[0][0].shape[0] == 5 and len(kept[3]) == 5  # only --Badprojections 1 removed
+    dropped = cli._load([p], *common, device=0, apply_found=True)
+    assert dropped[0][0].shape[0] == 3 and len(dropped[3]) == 3  # 1, 3 and 6 removed
+    assert cli.build_parser().parse_args([p, "--Apply_Found_Projections"]).Apply_Found_Projections
+    assert not cli.build_parser().parse_args([p]).Apply_Found_Projections
+
+
 def test_cli_option_handling(tmp_path):
     assert cli.parse_method("frob3d") == ("Frobenius 3D Reconstruction", 1)
     assert cli.parse_method("Uncorr2d") == ("Uncorrelated 2D Reconstruction", 0)
