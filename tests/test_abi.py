@@ -87,3 +87,14 @@ def test_error_mapping():
         L.check(L.GT_ERR_CUDA)
     with pytest.raises(TimeoutError):
         L.check(L.GT_ERR_TIMEOUT)
+
+
+def test_product_never_uses_the_oracle():
+    """The package's modules never import the oracle (it is test infrastructure)."""
+    pkg = os.path.join(ROOT, "graptor_gb300")
+    pat = re.compile(r"^\s*(import\s+oracle\b|from\s+oracle\b|from\s+\.\.oracle\b)", re.M)
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith(".py"):
+                with open(os.path.join(dirpath, f)) as fh:
+                    assert not pat.search(fh.read()), os.path.join(dirpath, f)
