@@ -20,6 +20,8 @@ collective on the data path; the time is the max over ranks.
 from __future__ import annotations
 
 import argparse
+import contextlib
+import io
 import json
 import os
 import statistics
@@ -709,8 +711,6 @@ def run_badproj(args, rank, world, local):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_steps = max(3, min(args.steps, 10))
-    import contextlib
-    import io
     for _ in range(e2e_steps):
         with contextlib.redirect_stdout(io.StringIO()):
             badproj.find_bad_projections("stack", None, 0.1, data=data, device=local)
