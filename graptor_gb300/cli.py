@@ -292,8 +292,25 @@ def coarse_section(levels_lo, levels_hi, p, refnew_y, refold_y, ny1, rounding):
     return z_, zu
 
 
+def subs_bad_projections(names, C0, badprojections, find_bad, device=0, apply_found=False):
+    """Per-resolution lists of projections to drop in the two-resolution driver:
+    ``badprojections[r]`` (r = 0 fine, 1 coarse), plus, with ``apply_found``, what
+    ``--Find_Bad_Projections`` finds in the first channel of that resolution."""
+    out = [list(b) for b in badprojections]
+    if find_bad[0] not in (0, 0.0):
+        if apply_found:
+            from . import badproj
+            for r, first in ((0, names[0]), (1, names[C0])):
+                out[r].extend(badproj.find_bad_projections(first, find_bad[1], find_bad[0], device=device))
+        else:
+            eprint("Warning: bad projections found by --Find_Bad_Projections are not applied in the subsampling "
+                   "reconstruction (--Apply_Found_Projections applies them).")
+    return out
+
+
 def reconstruct_subs(names, C0, result, mu, alpha, maxiter, method, levels, datahandling, badprojections, find_bad,
-                     channelnames, regularisation, discrepancy, pixelratio, overlay, chunksize, scalepars, device=0):
+                     channelnames, regularisation, discrepancy, pixelratio, overlay, chunksize, scalepars, device=0,
+                     apply_found=False):
     """Joint reconstruction from fine (``names[:C0]``) and coarse (``names[C0:]``)
     projection data (Coupled_Reconstruction3dbigresu, Reconstruction_coupled.py:542-873).
 
@@ -308,16 +325,16 @@ def reconstruct_subs(names, C0, result, mu, alpha, maxiter, method, levels, data
     As in the reference, bad projections found by ``--Find_Bad_Projections`` are not
     applied here (the reference appends them as a third, unread entry of the
     per-resolution list), and the coarse channels' fine-grid sinograms are all divided
-    by the last coarse channel's factor."""
+    by the last coarse channel's factor.  ``apply_found`` (``--Apply_Found_Projections``)
+    searches the first channel of each resolution and removes the projections found
+    from that resolution's channels."""
     from .radon_tgv_primal_dual_3dsubsample import Reconstructionapproach3dsubsmapling
     brightness, baseline, cutedges, badfile, threshold = datahandling[:5]
     C = len(names)
     C1 = C - C0
     if C0 < 1 or C1 < 1:
         raise ValueError("subsampling needs at least one fine and one coarse channel")
-    if find_bad[0] not in (0, 0.0):
-        eprint("Warning: bad projections found by --Find_Bad_Projections are not applied in the subsampling "
-               "reconstruction.")
+    badprojections = subs_bad_projections(names, C0, badprojections, find_bad, device, apply_found)
     data, angles, noise, sizes = [], [], [], []
     for n in names:
         r = int(n in names[C0:])
@@ -525,7 +542,7 @@ def main(argv=None):
         handling = [[dh[k], dh2[k]] for k in range(5)]
         u = reconstruct_subs(names, C0, args.Outfile, mu, alpha, args.Maxiter, method, levels, handling,
                              [list(args.Badprojections), list(args.Badprojections2)], find_bad, chn, reg, disc, pr,
-                             args.Overlapping, args.Chunksize, args.Scalepars, device)
+                             args.Overlapping, args.Chunksize, args.Scalepars, device, args.Apply_Found_Projections)
     elif setting == 1:
         u = reconstruct_3d(names, args.Outfile, mu, alpha, args.Maxiter, method, levels, dh, args.Badprojections,
                            find_bad, chn, reg, disc, args.Overlapping, args.Chunksize, args.Scalepars, device,

@@ -249,6 +249,10 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const __nv_bfloat16 *__restri
   }
   gt::tc_fence_before();
   __syncthreads();
+  // On the error path (a bounded wait gave up) the block does not know that the
+  // MMA it waited for has finished when it frees the tensor memory below; the
+  // wait limit is far above any MMA's duration, so this path is not expected to
+  // occur, and the error flag makes the host discard the whole launch's output.
   if (warp == 0) gt::tmem_dealloc(tmem, ncols);
 }
 

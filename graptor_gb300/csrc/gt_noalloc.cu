@@ -14,16 +14,23 @@
 // The array is GT_NOALLOC_SCRATCH_DOUBLES doubles (8 MiB).  Every GPU that loads
 // this library keeps it for the life of the process.  All calls share it and it
 // keeps the last call's contents (every call rewrites what it reads before
-// reading it), so calls whose GPU work overlaps -- different streams or host
-// threads on one device -- race on it; serialise them.
+// reading it).
 //
-// The first call on a device, with that device current, looks up the array's
-// device address (cudaGetSymbolAddress) and caches it; make that first call
-// before any stream capture.
+// Every call is host-synchronous: it ends by synchronising `stream` and copying
+// the estimate to the host, so it blocks until its GPU work is done and must
+// never be made on a stream that is being captured into a CUDA graph.  Two calls
+// therefore overlap on the GPU only when host threads call concurrently for the
+// same device (or other work on that device touches the array); they then race on
+// the scratch, so such threads must serialise their calls.
+//
+// Each call looks up the array's device address on the device it runs on
+// (cudaGetSymbolAddress, with that device current) and passes that address to the
+// kernels; it does not cache it, so a call made after cudaDeviceReset uses the
+// array of the new context.  The first call on a device also loads the library's
+// device code there.  The caller's current device is restored before returning.
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <mutex>
 
 #include "graptor_gb300.h"
 #include "gt_common.cuh"
@@ -38,7 +45,6 @@ int cuda_error(cudaError_t e, const char *what, int line);
 
 #define GT_NOALLOC_SCRATCH_DOUBLES (1u << 20)
 #define GT_NOALLOC_PARTIALS 256
-#define GT_NOALLOC_MAX_DEVICES 64
 
 // In host code this name is only a host-side handle: its device address comes
 // from cudaGetSymbolAddress below.
@@ -46,39 +52,21 @@ static __device__ __align__(256) double g_noalloc_scratch[GT_NOALLOC_SCRATCH_DOU
 
 namespace {
 
-std::mutex g_sym_mu;
-double *g_sym_ptr[GT_NOALLOC_MAX_DEVICES] = {nullptr};
-
-// device address of the scratch array on the current device (set-up on first use)
-int scratch_on(int device, double **out) {
-  if (device < 0 || device >= GT_NOALLOC_MAX_DEVICES) return gt::set_error(GT_ERR_ARG, "device ordinal out of range");
-  std::lock_guard<std::mutex> lk(g_sym_mu);
-  if (!g_sym_ptr[device]) {
-    void *ptr = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess) return gt::cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __LINE__);
-    g_sym_ptr[device] = static_cast<double *>(ptr);
-  }
-  *out = g_sym_ptr[device];
+// device address of the scratch array on the current device
+int scratch_here(double **out) {
+  void *ptr = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess) return gt::cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __LINE__);
+  *out = static_cast<double *>(ptr);
   return GT_OK;
 }
 
-}  // namespace
-
-extern "C" int gt_normest_noalloc(const double *angles, int N, int nd, int nang, int device, void *stream,
-                                  double *out) {
-  if (!angles || !out) return gt::set_error(GT_ERR_ARG, "gt_normest_noalloc: null argument");
-  if (N < 1 || nd < 1 || nang < 1) return gt::set_error(GT_ERR_ARG, "gt_normest_noalloc: sizes must be positive");
-  const size_t need = 4 * (size_t)nang + (size_t)N * N + (size_t)nd * nang + GT_NOALLOC_PARTIALS;
-  if (need > GT_NOALLOC_SCRATCH_DOUBLES)
-    return gt::set_error(GT_ERR_ARG,
-                         "gt_normest_noalloc: 4*nang + N*N + nd*nang + 256 must not exceed 1048576 doubles "
-                         "(the fixed 8 MiB scratch); use gt_problem_create/gt_set_data for larger geometries");
-  cudaError_t e = cudaSetDevice(device);
-  if (e != cudaSuccess) return gt::cuda_error(e, "cudaSetDevice", __LINE__);
+// the estimate on the current device (the entry point below selects it)
+int normest_here(const double *angles, int N, int nd, int nang, void *stream, double *out) {
   double *base = nullptr;
-  int rc = scratch_on(device, &base);
+  int rc = scratch_here(&base);
   if (rc) return rc;
+  cudaError_t e;
   cudaStream_t st = (cudaStream_t)stream;
   dvec4 *ofs = reinterpret_cast<dvec4 *>(base);
   double *img = base + 4 * (size_t)nang, *sino = img + (size_t)N * N, *part = sino + (size_t)nd * nang;
@@ -112,4 +100,30 @@ extern "C" int gt_normest_noalloc(const double *angles, int N, int nd, int nang,
   if (!(ne > 0) || !std::isfinite(ne)) return gt::set_error(GT_ERR_CUDA, "gt_normest_noalloc: estimate failed");
   *out = ne;
   return GT_OK;
+}
+
+}  // namespace
+
+extern "C" int gt_normest_noalloc(const double *angles, int N, int nd, int nang, int device, void *stream,
+                                  double *out) {
+  if (!angles || !out) return gt::set_error(GT_ERR_ARG, "gt_normest_noalloc: null argument");
+  if (N < 1 || nd < 1 || nang < 1) return gt::set_error(GT_ERR_ARG, "gt_normest_noalloc: sizes must be positive");
+  const size_t need = 4 * (size_t)nang + (size_t)N * N + (size_t)nd * nang + GT_NOALLOC_PARTIALS;
+  if (need > GT_NOALLOC_SCRATCH_DOUBLES)
+    return gt::set_error(GT_ERR_ARG,
+                         "gt_normest_noalloc: 4*nang + N*N + nd*nang + 256 must not exceed 1048576 doubles "
+                         "(the fixed 8 MiB scratch); use gt_problem_create/gt_set_data for larger geometries");
+  int caller = 0;
+  cudaError_t e = cudaGetDevice(&caller);
+  if (e != cudaSuccess) return gt::cuda_error(e, "cudaGetDevice", __LINE__);
+  if (caller != device && (e = cudaSetDevice(device)) != cudaSuccess) {
+    const int rc = gt::cuda_error(e, "cudaSetDevice", __LINE__);
+    cudaSetDevice(caller);
+    return rc;
+  }
+  const int rc = normest_here(angles, N, nd, nang, stream, out);
+  // the caller's current device is left as it was, on success and on error alike
+  if (caller != device && (e = cudaSetDevice(caller)) != cudaSuccess && rc == GT_OK)
+    return gt::cuda_error(e, "cudaSetDevice (restoring the caller's device)", __LINE__);
+  return rc;
 }

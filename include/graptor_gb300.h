@@ -170,9 +170,14 @@ GT_API int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n);
  * scratch is a fixed 8 MiB device array inside the library (kept by every GPU
  * that loads the library until the process exits).
  * Limit: 4*nang + N*N + nd*nang + 256 <= 1048576 (doubles); larger geometries
- * return GT_ERR_ARG.  Calls share the scratch, so calls whose GPU work overlaps
- * race; serialise them.  The first call on a device sets up the scratch address
- * for that device: make it before any stream capture. */
+ * return GT_ERR_ARG.  Every call is host-synchronous: it synchronises `stream`
+ * and copies the estimate to the host before returning, so it blocks the calling
+ * thread and must never be made on a stream that is being captured.  Calls share
+ * the scratch: calls from concurrent host threads for one device race on it, so
+ * serialise them.  Each call looks up the scratch's device address afresh (valid
+ * after cudaDeviceReset too); the first call on a device also loads the library's
+ * device code there.  The caller's current device is unchanged on return, on
+ * success and on error. */
 GT_API int gt_normest_noalloc(const double *angles, int N, int nd, int nang, int device, void *stream, double *out);
 
 /* Batches of independent problems (uneven sizes, channels, angle sets,

@@ -11,8 +11,9 @@ NumPy generator (radon_tgv_primal_dual_3d.py:1019); :func:`run_2d` / :func:`run_
 seed it first and return the operator-norm estimate the run used, so that the
 same value can be handed to the implementation under test.
 
-Needs the reference checkout (``GRAPTOR_REFERENCE`` or the default path below):
-available where fixtures are generated, absent on GPU machines.
+Needs the reference checkout, named by the environment variable
+``GRAPTOR_REFERENCE`` (there is no default): available where fixtures are
+generated, absent on GPU machines.
 """
 from __future__ import annotations
 
@@ -24,11 +25,12 @@ import sys
 import numpy as np
 
 _SHIM = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_DIR = os.environ.get("GRAPTOR_REFERENCE", "/root/reference")
+# the reference checkout: required, no default path
+REFERENCE_DIR = os.environ.get("GRAPTOR_REFERENCE", "")
 
 
 def available() -> bool:
-    return os.path.isfile(os.path.join(REFERENCE_DIR, "radon_tgv_primal_dual_3d.py"))
+    return bool(REFERENCE_DIR) and os.path.isfile(os.path.join(REFERENCE_DIR, "radon_tgv_primal_dual_3d.py"))
 
 
 def _ensure_path():

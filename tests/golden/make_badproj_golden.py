@@ -2,8 +2,8 @@
 
     python tests/golden/make_badproj_golden.py
 
-Imports the reference's ``find_bad_ele.py`` (``GRAPTOR_REFERENCE``, default the
-reference checkout) with stand-ins for the modules it imports but does not use on
+Imports the reference's ``find_bad_ele.py`` from the checkout that the environment
+variable ``GRAPTOR_REFERENCE`` names (required) with stand-ins for the modules it imports but does not use on
 this path (``h5utilities`` -- only its ``Brightness_correction`` is called, and it
 is replaced by a function returning the seeded input stack -- ``mrcfile``,
 ``scipy.misc`` and ``matplotlib``), then records its helper outputs and
@@ -27,7 +27,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("GRAPTOR_REFERENCE", "/root/reference")
+REF = os.environ.get("GRAPTOR_REFERENCE", "")
+if not REF or not os.path.isfile(os.path.join(REF, "find_bad_ele.py")):
+    raise SystemExit("set GRAPTOR_REFERENCE to the reference checkout (the directory holding find_bad_ele.py)")
 
 
 def stacks():

@@ -115,6 +115,24 @@ def test_found_projections_reported_not_removed(tmp_path, monkeypatch):
     assert not cli.build_parser().parse_args([p]).Apply_Found_Projections
 
 
+def test_subsampling_driver_applies_found_projections_on_request(monkeypatch):
+    """Two-resolution driver: found projections are left in by default (as in the
+    reference) and added per resolution with --Apply_Found_Projections."""
+    calls = []
+
+    def fake(name, searchradius, prozent, device=0):
+        calls.append(name)
+        return [2] if name == "fine0" else [4, 5]
+
+    monkeypatch.setattr(badproj, "find_bad_projections", fake)
+    names, bad = ["fine0", "fine1", "coarse0"], [[1], [7]]
+    assert cli.subs_bad_projections(names, 2, bad, [0, 2.0]) == [[1], [7]] and calls == []
+    assert cli.subs_bad_projections(names, 2, bad, [0.1, 2.0]) == [[1], [7]] and calls == []
+    assert cli.subs_bad_projections(names, 2, bad, [0.1, 2.0], apply_found=True) == [[1, 2], [7, 4, 5]]
+    assert calls == ["fine0", "coarse0"]
+    assert bad == [[1], [7]]  # the caller's lists are not modified
+
+
 def test_cli_option_handling(tmp_path):
     assert cli.parse_method("frob3d") == ("Frobenius 3D Reconstruction", 1)
     assert cli.parse_method("Uncorr2d") == ("Uncorrelated 2D Reconstruction", 0)
