@@ -97,6 +97,8 @@ _SIGS = {
     "gt_set_tuning": (ctypes.c_int, [_P, _I, _I]),
     "gt_set_dual_shape": (ctypes.c_int, [_P, _I]),
     "gt_get_dual_shape": (ctypes.c_int, [_P]),
+    "gt_set_schedule": (ctypes.c_int, [_P, _I]),
+    "gt_get_schedule": (ctypes.c_int, [_P]),
     "gt_test_bp_stall": (ctypes.c_int, [_P, _I, ctypes.c_uint]),
     "gt_nn_conv3d": (ctypes.c_int, [_P, _I, _I, _I, _I, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P]),
     "gt_nn_flip_weights": (ctypes.c_int, [_P, _P, _I, _I, _I, _P]),

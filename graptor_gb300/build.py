@@ -19,7 +19,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "libgraptor_gb300.so")
 BUILD = os.path.join(PKG, "_build")
-SOURCES = ["gt_kernels.cu", "gt_api.cu", "gt_noalloc.cu", "gt_nn.cu", "gt_badproj.cu"]
+SOURCES = ["gt_kernels.cu", "gt_proj.cu", "gt_api.cu", "gt_noalloc.cu", "gt_nn.cu", "gt_badproj.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          f"-I{os.path.join(ROOT, 'include')}", "-diag-suppress", "1444"]

@@ -25,7 +25,7 @@ cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st);
 cudaError_t prepare_bp_tma();
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st);
 cudaError_t launch_bp(const IterParams &P, cudaStream_t st);
-cudaError_t launch_update(const IterParams &P, int tgv, cudaStream_t st);
+cudaError_t launch_update(const IterParams &P, int tgv, cudaStream_t st, int part);
 cudaError_t launch_radon(const float *img, float *sino, const float4 *ofs, int N, int nd, int nang, int S,
                          cudaStream_t st);
 cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, int N, int nd, int nang, int S,
@@ -53,6 +53,8 @@ cudaError_t launch_ray_fill(const float4 *ofs, int N, int nd, int nang, const lo
                             cudaStream_t st);
 cudaError_t launch_bp_table(const float4 *ofs, int N, int nd, int nang, int2 *tab, cudaStream_t st);
 cudaError_t launch_run_count(const float4 *ofs, int N, int nd, int nang, int *count, cudaStream_t st);
+size_t row_table_bytes(int N, int nang);
+cudaError_t launch_row_fill(const float4 *ofs, int N, int nd, int nang, int4 *tab, int *bad, cudaStream_t st);
 cudaError_t launch_run_fill(const float4 *ofs, int N, int nd, int nang, const long long *start, int4 *ent,
                             cudaStream_t st);
 int num_proj_configs(int S, int which);
@@ -173,6 +175,7 @@ struct gt_problem {
   float *lam = nullptr, *f = nullptr, *ku = nullptr, *stage = nullptr, *kstar = nullptr;
   void *rays = nullptr;        // ray table (offsets + entries), built at creation
   void *runs = nullptr;        // 3-bin run table (offsets + entries), built at creation
+  void *tiles = nullptr;       // row-tile table of k_bp_row, built at creation
   size_t ray_bytes = 0;
   void *gap_ws = nullptr;      // gap workspace (v~ planes + FP64 block partials), allocated on first gt_gap
   double *mu64 = nullptr;
@@ -180,6 +183,8 @@ struct gt_problem {
   bool autotune = true;
   cudaGraphExec_t g_one = nullptr, g_chunk = nullptr;
   int chunk = 16;
+  int schedule = 1;            // 1: p / pbar half of the primal update beside the projectors; 0: one update after them
+  bool schedule_set = false;   // chosen by gt_set_schedule (the autotuner leaves it)
   long long iters = 0;
   bool has_data = false;
   double lsqr = 0;             // > 0: step-size constant of a variant (two-resolution solver: 36)
@@ -193,16 +198,22 @@ namespace {
 // One iteration as a fork/join.  The projector chain k_fwd -> k_bp (issue- and
 // cache-bound) needs only ubar and lambda; k_dual (DRAM-bound) needs ubar, pbar,
 // v, w; they write disjoint fields, so they run on two streams and overlap.
-// k_update waits for both.
+// The p / pbar half of the primal update (update_p and its extrapolation) needs
+// only k_dual's v and w, so it follows k_dual on the main stream, beside the
+// projectors; the u / ubar half needs K* lambda and waits for both streams.
+// Schedule 0 runs the whole primal update after the join.  Both schedules compute
+// every value by the same operations (bit-identical iterates).
 int enqueue_iteration(gt_problem *p) {
+  const int tgv = p->reg == GT_TGV;
   CK(cudaEventRecord(p->ev_fork, p->stream));
   CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
   CK(gt::launch_fwd(p->P, p->disc, p->side));
   CK(gt::launch_bp(p->P, p->side));
-  CK(gt::launch_dual(p->P, p->reg == GT_TGV, p->cpl, p->stream));
+  CK(gt::launch_dual(p->P, tgv, p->cpl, p->stream));
+  if (p->schedule == 1) CK(gt::launch_update(p->P, tgv, p->stream, 2));
   CK(cudaEventRecord(p->ev_join, p->side));
   CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
-  CK(gt::launch_update(p->P, p->reg == GT_TGV, p->stream));
+  CK(gt::launch_update(p->P, tgv, p->stream, p->schedule == 1 ? 1 : 0));
   return GT_OK;
 }
 
@@ -266,7 +277,7 @@ void set_scalars(gt_problem *p) {
 // launches never touch the solve.
 using TuneKey = std::tuple<int, int, int, int, int, int, int, int, int, int>;
 std::mutex g_tune_mu;
-std::map<TuneKey, std::tuple<int, int, int>> g_tune;
+std::map<TuneKey, std::tuple<int, int, int, int>> g_tune;
 
 int autotune(gt_problem *p) {
   const bool tgv = p->reg == GT_TGV;
@@ -289,7 +300,9 @@ int autotune(gt_problem *p) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
     if (it != g_tune.end()) {
-      std::tie(p->P.fwd_cfg, p->P.bp_cfg, p->P.dual_cfg) = it->second;
+      int sched = 0;
+      std::tie(p->P.fwd_cfg, p->P.bp_cfg, p->P.dual_cfg, sched) = it->second;
+      if (!p->schedule_set) p->schedule = sched;
       return GT_OK;
     }
   }
@@ -339,14 +352,45 @@ int autotune(gt_problem *p) {
       for (int c = 0; c < nc[which] && nc[which] > 1; ++c)
         fprintf(stderr, "graptor autotune %s cfg %d: %.4f ms%s\n", names[which], c, ms_cfg[which][c],
                 c == best[which] ? " *" : "");
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (rc) return rc;
+  if (rc) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
   p->P.fwd_cfg = best[0];
   p->P.bp_cfg = best[1];
   p->P.dual_cfg = best[2];
+  // the schedule (TGV only: TV has no p / pbar half): graph-captured iterations of
+  // each, the faster kept; concurrency between the kernels decides, not their times alone
+  if (tgv && !p->schedule_set) {
+    float ms_s[2] = {1e30f, 1e30f};
+    for (int round = 0; round < 2 && rc == GT_OK; ++round) {
+      for (int sched = 0; sched < 2 && rc == GT_OK; ++sched) {
+        p->schedule = sched;
+        cudaGraphExec_t g = nullptr;
+        rc = capture(p, 8, &g);
+        if (rc) break;
+        cudaError_t e = cudaGraphLaunch(g, p->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, p->stream);
+        for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = cudaGraphLaunch(g, p->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, p->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        cudaGraphExecDestroy(g);
+        if (e != cudaSuccess) { rc = cuda_err(e, "autotune (schedule)", __LINE__); break; }
+        ms_s[sched] = std::min(ms_s[sched], ms / 16);
+      }
+    }
+    p->schedule = ms_s[1] < ms_s[0] ? 1 : 0;
+    if (log && rc == GT_OK)
+      fprintf(stderr, "graptor autotune schedule 0: %.4f ms, 1: %.4f ms per iteration\n", ms_s[0], ms_s[1]);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune[key] = std::make_tuple(best[0], best[1], best[2]);
+  g_tune[key] = std::make_tuple(best[0], best[1], best[2], p->schedule);
   return GT_OK;
 }
 
@@ -365,7 +409,19 @@ const char *gt_version(void) { return "graptor_gb300 0.1 (sm_103a)"; }
 
 int gt_launches_per_iteration(const gt_problem *p) {
   if (!p) return 0;
-  return 3 + (p->d.C > 8 ? (p->d.C + 7) / 8 : 1);
+  return 3 + (p->d.C > 8 ? (p->d.C + 7) / 8 : 1) + (p->schedule == 1 && p->reg == GT_TGV ? 1 : 0);
+}
+
+int gt_set_schedule(gt_problem *p, int schedule) {
+  if (!p) return set_err(GT_ERR_ARG, "null argument");
+  if (schedule != 0 && schedule != 1) return set_err(GT_ERR_ARG, "schedule must be 0 or 1 (got %d)", schedule);
+  CK(cudaSetDevice(p->device));
+  CK(cudaStreamSynchronize(p->stream));
+  p->schedule = schedule;
+  p->schedule_set = true;
+  if (p->g_one) { cudaGraphExecDestroy(p->g_one); p->g_one = nullptr; }
+  if (p->g_chunk) { cudaGraphExecDestroy(p->g_chunk); p->g_chunk = nullptr; }
+  return GT_OK;
 }
 
 int gt_problem_create(const gt_desc *desc, gt_problem **out) {
@@ -539,6 +595,31 @@ int gt_problem_create(const gt_desc *desc, gt_problem **out) {
     }
   }
 
+  // row-tile table of the register-blocked back projector (k_bp_row); optional:
+  // without it (no memory, nd < 2, a geometry the table cannot describe) those
+  // launch shapes fall back to the others
+  if (D.nd >= 2) {
+    const size_t tbytes = gt::row_table_bytes(D.N, D.nang);
+    if (cudaMalloc(&p->tiles, align256(tbytes) + 256) == cudaSuccess) {
+      int *d_bad = (int *)((char *)p->tiles + align256(tbytes));
+      int bad = 0;
+      if ((e = cudaMemsetAsync(d_bad, 0, sizeof(int), p->stream)) != cudaSuccess ||
+          (e = gt::launch_row_fill(p->ofs, D.N, D.nd, D.nang, (int4 *)p->tiles, d_bad, p->stream)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, p->stream)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(p->stream)) != cudaSuccess)
+        return fail(cuda_err(e, "row table fill", __LINE__));
+      if (!bad) {
+        p->P.row_ent = (const int4 *)p->tiles;
+      } else {  // some lower bins do not step by 0 / 1 along a row: not used
+        cudaFree(p->tiles);
+        p->tiles = nullptr;
+      }
+    } else {
+      cudaGetLastError();
+      p->tiles = nullptr;
+    }
+  }
+
   gt::IterParams &P = p->P;
   P.d = p->d;
   P.ofs = p->ofs; P.mu = p->mu_eff;
@@ -567,6 +648,7 @@ void gt_problem_destroy(gt_problem *p) {
   if (p->block) cudaFree(p->block);
   if (p->rays) cudaFree(p->rays);
   if (p->runs) cudaFree(p->runs);
+  if (p->tiles) cudaFree(p->tiles);
   if (p->gap_ws) cudaFree(p->gap_ws);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
@@ -790,6 +872,8 @@ int gt_set_dual_shape(gt_problem *p, int cfg) {
 
 int gt_get_dual_shape(gt_problem *p) { return p ? p->P.dual_cfg : -1; }
 
+int gt_get_schedule(gt_problem *p) { return p ? p->schedule : -1; }
+
 int gt_test_bp_stall(gt_problem *p, int angle, unsigned wait_limit) {
   if (!p || wait_limit == 0) return set_err(GT_ERR_ARG, "invalid argument");
   CK(cudaSetDevice(p->device));
@@ -865,9 +949,12 @@ int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n) {
   if (!p || !ms_out || reps < 1 || n < 4) return set_err(GT_ERR_ARG, "bad argument");
   if (!p->has_data) return set_err(GT_ERR_STATE, "gt_time_kernels before gt_set_data");
   CK(cudaSetDevice(p->device));
-  cudaEvent_t ev[5];
+  // n >= 6: the primal update as its two halves (u / ubar, then p / pbar), timed
+  // separately into ms_out[4], ms_out[5], and ms_out[3] = their sum
+  const bool halves = n >= 6;
+  cudaEvent_t ev[6];
   for (auto &e : ev) CK(cudaEventCreate(&e));
-  float acc[4] = {0, 0, 0, 0};
+  float acc[5] = {0, 0, 0, 0, 0};
   int rc = GT_OK;
   const bool tgv = p->reg == GT_TGV;
   for (int r = 0; r < reps && rc == GT_OK; ++r) {
@@ -878,11 +965,13 @@ int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n) {
     if (e == cudaSuccess) e = cudaEventRecord(ev[2], p->stream);
     if (e == cudaSuccess) e = gt::launch_bp(p->P, p->stream);
     if (e == cudaSuccess) e = cudaEventRecord(ev[3], p->stream);
-    if (e == cudaSuccess) e = gt::launch_update(p->P, tgv, p->stream);
+    if (e == cudaSuccess) e = gt::launch_update(p->P, tgv, p->stream, halves ? 1 : 0);
     if (e == cudaSuccess) e = cudaEventRecord(ev[4], p->stream);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
+    if (halves && e == cudaSuccess) e = gt::launch_update(p->P, tgv, p->stream, 2);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[5], p->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
     if (e != cudaSuccess) { rc = cuda_err(e, "kernel timing", __LINE__); break; }
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 5; ++k) {
       float ms = 0;
       cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
       acc[k] += ms;
@@ -891,7 +980,12 @@ int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n) {
   }
   for (auto &e : ev) cudaEventDestroy(e);
   if (rc) return rc;
-  for (int k = 0; k < 4; ++k) ms_out[k] = acc[k] / reps;
+  for (int k = 0; k < 3; ++k) ms_out[k] = acc[k] / reps;
+  ms_out[3] = (acc[3] + acc[4]) / reps;
+  if (halves) {
+    ms_out[4] = acc[3] / reps;
+    ms_out[5] = acc[4] / reps;
+  }
   return GT_OK;
 }
 
@@ -1180,10 +1274,12 @@ int subs_iteration(gt_subs *s) {
   CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
   int rc = subs_projections(s, p->side);
   if (rc) return rc;
-  CK(gt::launch_dual(p->P, p->reg == GT_TGV, p->cpl, p->stream));
+  const int tgv = p->reg == GT_TGV;
+  CK(gt::launch_dual(p->P, tgv, p->cpl, p->stream));
+  if (p->schedule == 1) CK(gt::launch_update(p->P, tgv, p->stream, 2));
   CK(cudaEventRecord(p->ev_join, p->side));
   CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
-  CK(gt::launch_update(p->P, p->reg == GT_TGV, p->stream));
+  CK(gt::launch_update(p->P, tgv, p->stream, p->schedule == 1 ? 1 : 0));
   return GT_OK;
 }
 

@@ -49,6 +49,7 @@ struct IterParams {
   const long long *run_start;  // [nang*ceil(nd/3) + 1] offsets of the 3-bin run table (null: none)
   const int4 *run_ent;         // (pixel, weight bits of bins i0, i0+1, i0+2) entries of all runs
   const int2 *bp_tab;          // [N*N][nang] (floor bin, fraction bits) of the back projection (or null)
+  const int4 *row_ent;           // [N][ceil(N/4)][nang][3] back-projection row-tile entries (or null)
   const float *mu;       // [C] mu (KL) or mu/(sigma+mu) (L2)
   float *u, *ubar;       // [vol]
   float *p, *pbar, *v;   // [K][vol]

@@ -22,6 +22,7 @@
 #include <cmath>
 
 #include "gt_common.cuh"
+#include "gt_geom.cuh"
 #include "gt_tma.cuh"
 
 namespace gt {
@@ -1128,27 +1129,6 @@ static inline long long threads_for_wl(long long units, int S) { return units * 
 // acc = sum over rows y and x in [x_low, x_high] of (1 - |x X + y Y + off - i|)+ img.
 // The arithmetic is the reference's, in its order and without contraction.
 // ===========================================================================
-__device__ __forceinline__ void ray_rows(const float4 o, int i, int N, int &ylo, int &yhi) {
-  // rows whose x-extent [0, N-1] can reach detector coordinate (i-1, i+1); a
-  // conservative superset (the per-row bounds below decide exactly).
-  ylo = 0; yhi = N - 1;
-  if (fabsf(o.y) < 1e-3f) return;
-  const float tx = (float)(N - 1) * o.x;
-  const float tmin = fminf(0.f, tx), tmax = fmaxf(0.f, tx);
-  float ya, yb;
-  if (o.y > 0.f) {
-    ya = ((float)(i - 1) - o.z - tmax) / o.y;
-    yb = ((float)(i + 1) - o.z - tmin) / o.y;
-  } else {
-    ya = ((float)(i + 1) - o.z - tmin) / o.y;
-    yb = ((float)(i - 1) - o.z - tmax) / o.y;
-  }
-  ya = fminf(fmaxf(ya, -2.f), (float)N + 1.f);
-  yb = fminf(fmaxf(yb, -2.f), (float)N + 1.f);
-  ylo = max(0, (int)floorf(ya) - 1);
-  yhi = min(N - 1, (int)ceilf(yb) + 1);
-}
-
 template <int VW>
 __device__ __forceinline__ void radon_ray(const float *__restrict__ img, size_t S, int N, const float4 o, int i,
                                           const Slices<VW> &sl, float (&acc)[VW]) {
@@ -1587,16 +1567,21 @@ __device__ __forceinline__ void radon_ad_table(const float *__restrict__ lam, si
 
 // update_u (3-D :706-729, 2-D :340-357) + update_p (3-D :734-757, 2-D :359-376) +
 // extrapolation and swap (:1217-1221) for UW consecutive slices from s0.
-template <int DIM, bool TGV, int UW>
+// PART selects the halves: PART_U the u / ubar half (needs K* lambda), PART_P the
+// p / pbar half (needs only the dual kernel's v and w), PART_ALL both.  Each half
+// computes its values by the same operations whichever way it is launched.
+enum { PART_ALL = 0, PART_U = 1, PART_P = 2 };
+template <int DIM, bool TGV, int UW, int PART = PART_ALL>
 __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y, int s0, const float (&kstar)[UW]) {
   const Dims d = P.d;
   const size_t S = d.S, rowS = (size_t)d.N * S, vol = d.vol, i = ((size_t)y * d.N + x) * S + s0;
   int z[UW];
 #pragma unroll
   for (int k = 0; k < UW; ++k) z[k] = (DIM == 3) ? (s0 + k) % d.Nz : 0;
-
-  // divergence of v: backward differences (adjoint of the forward gradient)
   const float *__restrict__ v = P.v;
+
+  if (PART != PART_P) {
+  // divergence of v: backward differences (adjoint of the forward gradient)
   float a[UW], b[UW], am[UW], bm[UW], uo[UW], un[UW], ub[UW];
   ldw<UW>(v + i, a);
   ldw<UW>(v + vol + i, b);
@@ -1631,8 +1616,9 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
   }
   stv<UW>(P.ubar + i, ub);
   stv<UW>(P.u + i, un);
+  }
 
-  if (TGV) {
+  if (TGV && PART != PART_U) {
     const float *__restrict__ w = P.w;
     constexpr int K = DIM;
     // rows of the symmetric tensor: 3-D (w0 w3 w4), (w3 w1 w5), (w4 w5 w2); 2-D (w0 w2), (w2 w1)
@@ -1933,8 +1919,9 @@ cudaError_t prepare_bp_tma() {
                               (int)((size_t)BPT_ST * BPT_BINS * 256 * sizeof(float)));
 }
 
-// k_update: update_u + update_p + extrapolation for UW consecutive slices.
-template <int DIM, bool TGV, int UW>
+// k_update: update_u + update_p + extrapolation for UW consecutive slices (PART:
+// both halves, or one of them, see primal_update).
+template <int DIM, bool TGV, int UW, int PART = PART_ALL>
 __global__ void __launch_bounds__(256) k_update(const IterParams P) {
   const Dims d = P.d;
   const int nsg = d.S / UW;
@@ -1944,8 +1931,8 @@ __global__ void __launch_bounds__(256) k_update(const IterParams P) {
   const int s0 = (int)(t - (long long)pix * nsg) * UW;
   const int y = pix / d.N, x = pix - y * d.N;
   float ks[UW];
-  ldw<UW>(P.kstar + (size_t)pix * d.S + s0, ks);
-  primal_update<DIM, TGV, UW>(P, x, y, s0, ks);
+  if (PART != PART_P) ldw<UW>(P.kstar + (size_t)pix * d.S + s0, ks);
+  primal_update<DIM, TGV, UW, PART>(P, x, y, s0, ks);
 }
 
 // ===========================================================================
@@ -2802,12 +2789,14 @@ static inline int vec_width(int S) { return (S % 4 == 0) ? 8 : (S % 2 == 0 ? 2 :
 // for images and sinograms larger than L2.  k_fwd configs 10, 11: the 3-bin run
 // table (k_fwd_rt) with (slices per lane, entries in flight) = (8, 4), (4, 8);
 // configs 12, 13: (8, 8) and (8, 4) with registers capped for 5 / 6 resident blocks.
+// k_bp configs 18, 19: the register-blocked row-tile kernel (gt_proj.cu) with 4 or
+// 2 slices per lane.
 // Otherwise one fixed shape with 2 or 1 slices per thread.
 // One more candidate each: one slice per thread (k_fwd config 4, k_bp config 8),
 // which keeps all lanes busy when S is small.
 int num_proj_configs(int S, int which) {
   if (S % 4 != 0) return 1;
-  return which == 0 ? 20 : 18;  // configs 4 / 8 (one slice per thread) stay candidates for every S
+  return which == 0 ? 20 : 20;  // configs 4 / 8 (one slice per thread) stay candidates for every S
 }
 
 template <int VW, int UNR>
@@ -2846,6 +2835,8 @@ static void fwd_run(const IterParams &P, int disc, cudaStream_t st) {
   if (disc == KL) k_fwd_run<KL, VW, R><<<g, 256, 0, st>>>(P);
   else k_fwd_run<L2, VW, R><<<g, 256, 0, st>>>(P);
 }
+
+cudaError_t launch_bp_row(const IterParams &P, int shape, cudaStream_t st);
 
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st) {
   const int S = P.d.S;
@@ -2908,6 +2899,12 @@ static void bp_run(const IterParams &P, cudaStream_t st) {
 
 cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
   const int S = P.d.S;
+  if (S % 4 == 0 && (P.bp_cfg == 18 || P.bp_cfg == 19)) {
+    // register-blocked row-tile kernel (gt_proj.cu); without its table the one-angle shape
+    if (P.row_ent) return launch_bp_row(P, P.bp_cfg - 18, st);
+    bp_vw<8, 1, false>(P, st);
+    return cudaGetLastError();
+  }
   if (S % 4 == 0) {
     switch (P.bp_cfg) {
       case 1: bp_vw<8, 4>(P, st); break;
@@ -2941,23 +2938,33 @@ cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int UW>
+template <int UW, int PART>
 static void update_uw(const IterParams &P, int tgv, cudaStream_t st) {
   const unsigned g = blocks_for((long long)P.d.N * P.d.N * (P.d.S / UW), 256);
   if (P.d.dim == 3) {
-    if (tgv) k_update<3, true, UW><<<g, 256, 0, st>>>(P);
-    else k_update<3, false, UW><<<g, 256, 0, st>>>(P);
+    if (tgv) k_update<3, true, UW, PART><<<g, 256, 0, st>>>(P);
+    else k_update<3, false, UW, PART_ALL><<<g, 256, 0, st>>>(P);
   } else {
-    if (tgv) k_update<2, true, UW><<<g, 256, 0, st>>>(P);
-    else k_update<2, false, UW><<<g, 256, 0, st>>>(P);
+    if (tgv) k_update<2, true, UW, PART><<<g, 256, 0, st>>>(P);
+    else k_update<2, false, UW, PART_ALL><<<g, 256, 0, st>>>(P);
   }
 }
 
-cudaError_t launch_update(const IterParams &P, int tgv, cudaStream_t st) {
+template <int PART>
+static void update_part(const IterParams &P, int tgv, cudaStream_t st) {
   const int S = P.d.S;
-  if (S % 4 == 0) update_uw<4>(P, tgv, st);
-  else if (S % 2 == 0) update_uw<2>(P, tgv, st);
-  else update_uw<1>(P, tgv, st);
+  if (S % 4 == 0) update_uw<4, PART>(P, tgv, st);
+  else if (S % 2 == 0) update_uw<2, PART>(P, tgv, st);
+  else update_uw<1, PART>(P, tgv, st);
+}
+
+// part: 0 both halves in one launch, 1 the u / ubar half, 2 the p / pbar half
+// (TV has no p: part 1 is the whole update and part 2 launches nothing)
+cudaError_t launch_update(const IterParams &P, int tgv, cudaStream_t st, int part) {
+  if (part == 2 && !tgv) return cudaSuccess;
+  if (part == 1) update_part<PART_U>(P, tgv, st);
+  else if (part == 2) update_part<PART_P>(P, tgv, st);
+  else update_part<PART_ALL>(P, tgv, st);
   return cudaGetLastError();
 }
 

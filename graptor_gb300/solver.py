@@ -142,6 +142,12 @@ class Problem:
         L.check(L.lib().gt_set_dual_shape(self._h, int(cfg)))
         return self
 
+    def set_schedule(self, schedule: int):
+        """1: the p / pbar half of the primal update beside the projectors (default);
+        0: the whole primal update after them (see gt_set_schedule)."""
+        L.check(L.lib().gt_set_schedule(self._h, int(schedule)))
+        return self
+
     def dual_from_primal(self, empty_weight: float = 1.0, cap: int = 0, repair: bool = False):
         """Set lambda consistent with the current u (for warm starts); bins
         without data move empty_weight of the way to their fixed point; cap 10
@@ -165,10 +171,12 @@ class Problem:
 
     @property
     def tuning(self) -> dict:
-        """Projector launch shapes the autotuner chose (see launch_fwd / launch_bp)."""
+        """Launch shapes and iteration schedule the autotuner chose (see launch_fwd /
+        launch_bp / gt_set_schedule)."""
         out = (ctypes.c_int * 2)()
         L.check(L.lib().gt_get_tuning(self._h, out))
-        return {"fwd_cfg": out[0], "bp_cfg": out[1], "dual_cfg": L.lib().gt_get_dual_shape(self._h)}
+        return {"fwd_cfg": out[0], "bp_cfg": out[1], "dual_cfg": L.lib().gt_get_dual_shape(self._h),
+                "schedule": L.lib().gt_get_schedule(self._h)}
 
     def gap(self, U: float = 0.0) -> dict:
         """FP64 primal-dual gap of the current iterate on the box u in [0, U] (U <= 0: 2 max u)."""
@@ -224,10 +232,12 @@ class Problem:
         return p
 
     def time_kernels(self, reps: int = 5) -> dict:
-        """Mean CUDA-event duration (ms) of each kernel of one iteration."""
-        out = (ctypes.c_float * 4)()
-        L.check(L.lib().gt_time_kernels(self._h, int(reps), out, 4))
-        return {"k_dual": out[0], "k_fwd": out[1], "k_bp": out[2], "k_update": out[3]}
+        """Mean CUDA-event duration (ms) of each kernel of one iteration; the
+        primal update as a whole (k_update) and as its u / ubar and p / pbar halves."""
+        out = (ctypes.c_float * 6)()
+        L.check(L.lib().gt_time_kernels(self._h, int(reps), out, 6))
+        return {"k_dual": out[0], "k_fwd": out[1], "k_bp": out[2], "k_update": out[3], "k_update_u": out[4],
+                "k_update_p": out[5]}
 
     @property
     def launches_per_iteration(self) -> int:

@@ -118,6 +118,16 @@ GT_API int gt_set_tuning(gt_problem *p, int fwd_cfg, int bp_cfg);
  * gt_get_dual_shape returns the current one. */
 GT_API int gt_set_dual_shape(gt_problem *p, int cfg);
 GT_API int gt_get_dual_shape(gt_problem *p);
+/* Iteration schedule.  1: the p / pbar half of the primal update (update_p +
+ * its extrapolation, radon_tgv_primal_dual_3d.py:734-757, :1217-1221) runs right
+ * after the dual update, beside the projector chain, and only the u / ubar half
+ * (update_u, :706-729) waits for the back projection; 0: the whole primal update
+ * runs after the back projection.  The reference enqueues update_u then update_p
+ * after radon_ad (:1194-1221); both schedules give bit-identical iterates.  The
+ * autotuner (gt_set_data) times both as graph-captured iterations and keeps the
+ * faster, unless gt_set_schedule chose one; gt_get_schedule returns the current. */
+GT_API int gt_set_schedule(gt_problem *p, int schedule);
+GT_API int gt_get_schedule(gt_problem *p);
 
 /* Test hook of the TMA-staged back projection (back-projection shapes 14, 15):
  * its next launches never issue the copy of `angle` (a wait nothing completes)
@@ -154,8 +164,10 @@ GT_API int gt_radon_ad(const float *sino_dev, float *img_dev, const double *angl
 
 /* Run reps iterations kernel by kernel (not graph-captured, no overlap), timing
  * each kernel with CUDA events on the problem stream; ms_out[0..3] receive the
- * mean duration of k_dual, k_fwd, k_bp and k_update (n >= 4).  The iterations are
- * real: the state advances by reps iterations. */
+ * mean duration of k_dual, k_fwd, k_bp and k_update (n >= 4); with n >= 6 the
+ * update runs as its two halves, ms_out[4] and ms_out[5] receive the u / ubar and
+ * the p / pbar half and ms_out[3] their sum.  The iterations are real: the state
+ * advances by reps iterations. */
 GT_API int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n);
 
 /* Allocation-free operator-norm estimate.  No counterpart in the reference (which

@@ -209,23 +209,27 @@ def test_state_roundtrip_and_warm_start():
         assert p.scalars["normest"] == 15.0
 
 
-@pytest.mark.parametrize("S_case", [(40, 3, 2, 21), (36, 16, 1, 17), (41, 4, 2, 19)], ids=["S6", "S16", "S8odd"])
+@pytest.mark.parametrize("S_case", [(40, 3, 2, 21, 40), (36, 16, 1, 17, 36), (41, 4, 2, 19, 41), (38, 2, 2, 23, 45),
+                                    (27, 8, 1, 13, 22), (9, 4, 1, 31, 2)],
+                         ids=["S6", "S16", "S8odd", "S4nd45", "S8nd22", "S4nd2"])
 def test_projector_launch_shapes_give_identical_iterates(S_case):
     """Every forward / back projection launch shape the autotuner can pick sums the
-    same terms in the same order, so the iterates agree bit for bit."""
+    same terms in the same order, so the iterates agree bit for bit; this includes
+    the register-blocked row-tile back projector (18, 19), whose zero-weight
+    pairings leave every sum unchanged."""
+    from graptor_gb300 import _lib as L
     from graptor_gb300 import phantom
     from graptor_gb300.solver import Problem
-    N, Nz, C, nang = S_case
+    N, Nz, C, nang, nd = S_case
     rng = np.random.default_rng(zlib.crc32(repr(S_case).encode()))
-    ang = phantom.angles_deg(nang)
-    f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
+    ang = phantom.angles_deg(nang, -85, 95)
+    f = np.abs(rng.standard_normal((C * Nz, nang, nd))).astype(np.float32)
     ref = None
-    with Problem(3, N, Nz, C, N, ang, (4, 1), [0.2] * C, normest=17.0) as p:
+    with Problem(3, N, Nz, C, nd, ang, (4, 1), [0.2] * C, normest=17.0) as p:
         p.set_data(f)
-        from graptor_gb300 import _lib as L
         nf = L.lib().gt_set_tuning(p._h, 99, 0)
         assert nf != 0  # out of range is refused
-        configs = [(fc, 0) for fc in range(20)] + [(0, bc) for bc in range(1, 18)] if (C * Nz) % 4 == 0 else [(0, 0)]
+        configs = [(fc, 0) for fc in range(20)] + [(0, bc) for bc in range(1, 20)] if (C * Nz) % 4 == 0 else [(0, 0)]
         for fc, bc in configs:
             p.set_data(f)
             try:
@@ -262,14 +266,20 @@ def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg):
         shapes = (0, 2, 3, 4, 5, 6, 8)
     else:
         shapes = (0, 1, 2, 3, 4, 5, 6, 7, 8, 9) if z2 else (0, 2, 3, 4, 5, 6, 7, 8, 9)
-    fields = ("u", "v", "w", "p") if reg == "TGV" else ("u", "v")
+    fields = ("u", "ubar", "v", "w", "p", "pbar", "lambda") if reg == "TGV" else ("u", "ubar", "v", "lambda")
     with Problem(dim, N, Nz, C, N, ang, (4, 1), [0.3] * C, regularisation=reg, coupling=cpl, normest=17.0,
                  stepsize=2.0) as p:
         for shape in shapes:
-            p.set_data(f)
-            p.set_dual_shape(shape)
-            p.run(9).synchronize()
-            got.append({k: p.get(k) for k in fields})
+            # the primal update as one launch after the projectors (schedule 0) or as its
+            # p / pbar half beside them (schedule 1): the same values
+            for schedule in ((0, 1) if shape == shapes[-1] else (1,)):
+                p.set_schedule(schedule)
+                p.set_data(f)
+                p.set_dual_shape(shape)
+                p.run(9).synchronize()
+                got.append({k: p.get(k) for k in fields})
+        with pytest.raises(ValueError):
+            p.set_schedule(2)
         with pytest.raises(ValueError):
             p.set_dual_shape(10)
         if not z2:
