@@ -99,6 +99,11 @@ _SIGS = {
     "gt_get_dual_shape": (ctypes.c_int, [_P]),
     "gt_set_schedule": (ctypes.c_int, [_P, _I]),
     "gt_get_schedule": (ctypes.c_int, [_P]),
+    "gt_set_primal_weight": (ctypes.c_int, [_P, ctypes.c_double]),
+    "gt_get_primal_weight": (ctypes.c_double, [_P]),
+    "gt_restart": (ctypes.c_int, [_P]),
+    "gt_snapshot": (ctypes.c_int, [_P]),
+    "gt_movement": (ctypes.c_int, [_P, _P]),
     "gt_test_bp_stall": (ctypes.c_int, [_P, _I, ctypes.c_uint]),
     "gt_nn_conv3d": (ctypes.c_int, [_P, _I, _I, _I, _I, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P]),
     "gt_nn_flip_weights": (ctypes.c_int, [_P, _P, _I, _I, _I, _P]),

@@ -42,6 +42,7 @@ cudaError_t launch_csr_planes(const float *in, float *out, const int *start, con
 cudaError_t launch_lambda_update(float *lam, const float *ku, const float *f, const float *mu, float sigma,
                                  long long n, int S, int Nz, int disc, cudaStream_t st);
 cudaError_t launch_sumsq(const float *x, long long n, double *part, int nb, cudaStream_t st);
+cudaError_t launch_sqdiff(const float *a, const float *b, long long n, double *part, int nb, cudaStream_t st);
 cudaError_t launch_scale_f32(float *x, long long n, float s, cudaStream_t st);
 cudaError_t launch_add2(float *a, float *b, const float *d, long long n, cudaStream_t st);
 cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, double *d_img, double *d_sino,
@@ -178,6 +179,8 @@ struct gt_problem {
   void *tiles = nullptr;       // row-tile table of k_bp_row, built at creation
   size_t ray_bytes = 0;
   void *gap_ws = nullptr;      // gap workspace (v~ planes + FP64 block partials), allocated on first gt_gap
+  float *snap = nullptr;       // copy of (u, p, v, w, lambda) for gt_movement, allocated on first gt_snapshot
+  double pweight = 1.0;        // primal weight: sigma = w / sqrt(Lsqr), tau = 1 / (w sqrt(Lsqr)); 1 = reference
   double *mu64 = nullptr;
   gt::IterParams P{};
   bool autotune = true;
@@ -256,8 +259,9 @@ int field_info(gt_problem *p, int field, float **ptr, int *comps, size_t *X) {
 void set_scalars(gt_problem *p) {
   // tgv_radon :1178-1189 (3-D) / :753-762 (2-D)
   const double Lsqr = p->lsqr > 0 ? p->lsqr : (p->d.dim == 3 ? 17.0 : 0.5 * (18.0 + std::sqrt(33.0)));
-  p->sigma = 1.0 / std::sqrt(Lsqr);
-  p->tau = p->sigma;
+  // sigma tau Lsqr = 1 for every primal weight; weight 1 is the reference's sigma = tau
+  p->sigma = p->pweight / std::sqrt(Lsqr);
+  p->tau = 1.0 / (p->pweight * std::sqrt(Lsqr));
   const double ne2 = p->ne * p->ne;
   const double a0 = p->alpha0 / ne2, a1 = p->alpha1 / ne2;
   p->P.sigma = (float)p->sigma;
@@ -267,6 +271,16 @@ void set_scalars(gt_problem *p) {
   p->P.ainv0 = (float)(1.0 / a0);
   p->P.ainv1 = (float)(1.0 / a1);
   p->P.stepsize = p->stepsize;
+}
+
+// channel weights of the data-term prox: KL mu, L2 mu/(sigma+mu) (3-D :1186-1189)
+int upload_mu_eff(gt_problem *p) {
+  std::vector<float> me(p->d.C);
+  for (int c = 0; c < p->d.C; ++c)
+    me[c] = (float)(p->disc == GT_KL ? p->mu[c] : p->mu[c] / (p->sigma + p->mu[c]));
+  CK(cudaMemcpyAsync(p->mu_eff, me.data(), sizeof(float) * p->d.C, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaStreamSynchronize(p->stream));  // me is a host buffer
+  return GT_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -650,6 +664,7 @@ void gt_problem_destroy(gt_problem *p) {
   if (p->runs) cudaFree(p->runs);
   if (p->tiles) cudaFree(p->tiles);
   if (p->gap_ws) cudaFree(p->gap_ws);
+  if (p->snap) cudaFree(p->snap);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
   if (p->side) cudaStreamDestroy(p->side);
@@ -691,11 +706,10 @@ int gt_set_data(gt_problem *p, const float *f_host, int make_feasible) {
     p->ne = ne;
   }
   set_scalars(p);
-  // channel weights: KL mu, L2 mu/(sigma+mu) (3-D :1186-1189)
-  std::vector<float> me(d.C);
-  for (int c = 0; c < d.C; ++c)
-    me[c] = (float)(p->disc == GT_KL ? p->mu[c] : p->mu[c] / (p->sigma + p->mu[c]));
-  CK(cudaMemcpyAsync(p->mu_eff, me.data(), sizeof(float) * d.C, cudaMemcpyHostToDevice, p->stream));
+  {
+    const int rc = upload_mu_eff(p);
+    if (rc) return rc;
+  }
   CK(cudaMemcpyAsync(p->mu64, p->mu.data(), sizeof(double) * d.C, cudaMemcpyHostToDevice, p->stream));
   p->P.ne64 = p->ne;
   // pick the projector launch shapes (uses lambda / ku / kstar as scratch: they are reset below)
@@ -873,6 +887,101 @@ int gt_set_dual_shape(gt_problem *p, int cfg) {
 int gt_get_dual_shape(gt_problem *p) { return p ? p->P.dual_cfg : -1; }
 
 int gt_get_schedule(gt_problem *p) { return p ? p->schedule : -1; }
+
+int gt_set_primal_weight(gt_problem *p, double w) {
+  if (!p || !(w > 0) || !std::isfinite(w)) return set_err(GT_ERR_ARG, "primal weight must be positive and finite");
+  if (!p->has_data) return set_err(GT_ERR_STATE, "gt_set_primal_weight before gt_set_data");
+  CK(cudaSetDevice(p->device));
+  CK(cudaStreamSynchronize(p->stream));
+  p->pweight = w;
+  set_scalars(p);
+  const int rc = upload_mu_eff(p);
+  if (rc) return rc;
+  // the captured graphs hold the old step sizes
+  if (p->g_one) { cudaGraphExecDestroy(p->g_one); p->g_one = nullptr; }
+  if (p->g_chunk) { cudaGraphExecDestroy(p->g_chunk); p->g_chunk = nullptr; }
+  return GT_OK;
+}
+
+double gt_get_primal_weight(gt_problem *p) { return p ? p->pweight : 0.0; }
+
+int gt_restart(gt_problem *p) {
+  if (!p) return set_err(GT_ERR_ARG, "null argument");
+  if (!p->has_data) return set_err(GT_ERR_STATE, "gt_restart before gt_set_data");
+  CK(cudaSetDevice(p->device));
+  const size_t fv = sizeof(float) * p->d.vol;
+  CK(cudaMemcpyAsync(p->ubar, p->u, fv, cudaMemcpyDeviceToDevice, p->stream));
+  if (p->reg == GT_TGV) CK(cudaMemcpyAsync(p->pbar, p->p, fv * p->K, cudaMemcpyDeviceToDevice, p->stream));
+  return GT_OK;
+}
+
+namespace {
+constexpr int kMoveBlocks = 1024;  // FP64 partial sums per field of gt_movement
+
+// (pointer, element count) of the fields of a restart: primal u, p; dual v, w, lambda
+void restart_fields(gt_problem *p, float *fld[5], size_t n[5]) {
+  const size_t vol = p->d.vol;
+  const bool tgv = p->reg == GT_TGV;
+  fld[0] = p->u; n[0] = vol;
+  fld[1] = p->p; n[1] = tgv ? vol * p->K : 0;
+  fld[2] = p->v; n[2] = vol * p->K;
+  fld[3] = p->w; n[3] = tgv ? vol * p->KW : 0;
+  fld[4] = p->lam; n[4] = p->d.nbin;
+}
+}  // namespace
+
+int gt_snapshot(gt_problem *p) {
+  if (!p) return set_err(GT_ERR_ARG, "null argument");
+  if (!p->has_data) return set_err(GT_ERR_STATE, "gt_snapshot before gt_set_data");
+  CK(cudaSetDevice(p->device));
+  float *fld[5];
+  size_t n[5], total = 0;
+  restart_fields(p, fld, n);
+  for (size_t k : n) total += k;
+  if (!p->snap) {  // the fields, then the FP64 block partials of gt_movement
+    cudaError_t e = cudaMalloc(&p->snap, align256(sizeof(float) * total) + sizeof(double) * kMoveBlocks * 5);
+    if (e != cudaSuccess) { p->snap = nullptr; return cuda_err(e, "cudaMalloc (snapshot)", __LINE__); }
+  }
+  size_t off = 0;
+  for (int k = 0; k < 5; ++k) {
+    if (n[k]) CK(cudaMemcpyAsync(p->snap + off, fld[k], sizeof(float) * n[k], cudaMemcpyDeviceToDevice, p->stream));
+    off += n[k];
+  }
+  return GT_OK;
+}
+
+int gt_movement(gt_problem *p, double out[2]) {
+  if (!p || !out) return set_err(GT_ERR_ARG, "null argument");
+  if (!p->snap) return set_err(GT_ERR_STATE, "gt_movement before gt_snapshot");
+  CK(cudaSetDevice(p->device));
+  constexpr int nb = kMoveBlocks;
+  float *fld[5];
+  size_t n[5], total = 0;
+  restart_fields(p, fld, n);
+  for (size_t k : n) total += k;
+  double *part = (double *)((char *)p->snap + align256(sizeof(float) * total));
+  size_t off = 0;
+  int rc = GT_OK;
+  for (int k = 0; k < 5 && rc == GT_OK; ++k) {
+    cudaError_t e = n[k] ? gt::launch_sqdiff(fld[k], p->snap + off, (long long)n[k], part + nb * k, nb, p->stream)
+                         : cudaMemsetAsync(part + nb * k, 0, sizeof(double) * nb, p->stream);
+    if (e != cudaSuccess) rc = cuda_err(e, "movement", __LINE__);
+    off += n[k];
+  }
+  std::vector<double> h(nb * 5);
+  if (rc == GT_OK) {
+    cudaError_t e = cudaMemcpyAsync(h.data(), part, sizeof(double) * nb * 5, cudaMemcpyDeviceToHost, p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) rc = cuda_err(e, "movement", __LINE__);
+  }
+  if (rc) return rc;
+  double s[5] = {0, 0, 0, 0, 0};
+  for (int k = 0; k < 5; ++k)
+    for (int b = 0; b < nb; ++b) s[k] += h[(size_t)nb * k + b];
+  out[0] = std::sqrt(s[0] + s[1]);
+  out[1] = std::sqrt(s[2] + s[3] + s[4]);
+  return GT_OK;
+}
 
 int gt_test_bp_stall(gt_problem *p, int angle, unsigned wait_limit) {
   if (!p || wait_limit == 0) return set_err(GT_ERR_ARG, "invalid argument");

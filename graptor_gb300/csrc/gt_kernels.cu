@@ -2118,6 +2118,24 @@ __global__ void k_sumsq_partial(const float *__restrict__ x, long long n, double
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
+// sum of (a - b)^2 in FP64, block partials (restarted iterations: distance moved)
+__global__ void k_sqdiff_partial(const float *__restrict__ a, const float *__restrict__ b, long long n,
+                                 double *__restrict__ part) {
+  __shared__ double sh[256];
+  double acc = 0.0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const double v = (double)a[k] - (double)b[k];
+    acc += v * v;
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
 __global__ void k_scale_f32(float *__restrict__ x, long long n, float s) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) x[t] *= s;
@@ -2142,6 +2160,11 @@ cudaError_t launch_lambda_update(float *lam, const float *ku, const float *f, co
   k_lambda_update<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(lam, ku, f, mu, sigma, n, S, Nz, disc);
   return cudaGetLastError();
 }
+cudaError_t launch_sqdiff(const float *a, const float *b, long long n, double *part, int nb, cudaStream_t st) {
+  k_sqdiff_partial<<<nb, 256, 0, st>>>(a, b, n, part);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sumsq(const float *x, long long n, double *part, int nb, cudaStream_t st) {
   k_sumsq_partial<<<nb, 256, 0, st>>>(x, n, part);
   return cudaGetLastError();

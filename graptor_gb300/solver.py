@@ -142,6 +142,32 @@ class Problem:
         L.check(L.lib().gt_set_dual_shape(self._h, int(cfg)))
         return self
 
+    def set_primal_weight(self, w: float):
+        """Primal weight of the step pair: sigma = w / sqrt(Lsqr), tau = 1 / (w sqrt(Lsqr))
+        (1 = the reference's steps, the default; see gt_set_primal_weight)."""
+        L.check(L.lib().gt_set_primal_weight(self._h, float(w)))
+        return self
+
+    @property
+    def primal_weight(self) -> float:
+        return float(L.lib().gt_get_primal_weight(self._h))
+
+    def restart(self):
+        """Restart the extrapolation from the current point (ubar = u, pbar = p)."""
+        L.check(L.lib().gt_restart(self._h))
+        return self
+
+    def snapshot(self):
+        """Keep a copy of (u, p, v, w, lambda) for :meth:`movement`."""
+        L.check(L.lib().gt_snapshot(self._h))
+        return self
+
+    def movement(self) -> tuple:
+        """L2 distances of the primal (u, p) and dual (v, w, lambda) parts from the snapshot."""
+        out = (ctypes.c_double * 2)()
+        L.check(L.lib().gt_movement(self._h, out))
+        return float(out[0]), float(out[1])
+
     def set_schedule(self, schedule: int):
         """1: the p / pbar half of the primal update beside the projectors (default);
         0: the whole primal update after them (see gt_set_schedule)."""

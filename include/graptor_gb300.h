@@ -129,6 +129,22 @@ GT_API int gt_get_dual_shape(gt_problem *p);
 GT_API int gt_set_schedule(gt_problem *p, int schedule);
 GT_API int gt_get_schedule(gt_problem *p);
 
+/* Time-to-gap building blocks (restarted primal-dual iterations).  No
+ * counterpart in the reference, which always runs a fixed iteration count with
+ * sigma = tau = 1/sqrt(Lsqr) (radon_tgv_primal_dual_3d.py:1180-1184).
+ * gt_set_primal_weight: sigma = w/sqrt(Lsqr), tau = 1/(w sqrt(Lsqr)) (sigma tau
+ * Lsqr stays 1, so the iteration still converges); w = 1 is the reference's step
+ * pair and the default; kept across gt_set_data.  gt_restart: ubar = u, pbar = p
+ * (the extrapolation restarts from the current point).  gt_snapshot copies
+ * (u, p, v, w, lambda) aside (allocated on first use); gt_movement writes the L2
+ * distance of the primal (u, p) and dual (v, w, lambda) parts from that copy to
+ * out[0], out[1] (host-synchronous). */
+GT_API int gt_set_primal_weight(gt_problem *p, double w);
+GT_API double gt_get_primal_weight(gt_problem *p);
+GT_API int gt_restart(gt_problem *p);
+GT_API int gt_snapshot(gt_problem *p);
+GT_API int gt_movement(gt_problem *p, double out[2]);
+
 /* Test hook of the TMA-staged back projection (back-projection shapes 14, 15):
  * its next launches never issue the copy of `angle` (a wait nothing completes)
  * and poll at most `wait_limit` times per wait, so every block gives up, flags

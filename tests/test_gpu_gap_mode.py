@@ -1,0 +1,89 @@
+"""The time-to-gap building blocks through the C ABI: the primal weight of the
+step pair (sigma = w / sqrt(Lsqr), tau = 1 / (w sqrt(Lsqr))), restarts of the
+extrapolation and the distance moved since a snapshot.
+
+The primal weight changes only the step sizes of the reference iteration
+(radon_tgv_primal_dual_3d.py:1180-1189, :1194-1221), so the iterates must match
+the oracle run with the same steps; weight 1 is the reference's pair.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / (nb if nb > 0 else 1.0))
+
+
+def _case(disc, seed=11):
+    from graptor_gb300 import phantom
+    from oracle import oracle as O
+    N, Nz, C, nang = 28, 4, 2, 19
+    rng = np.random.default_rng(seed)
+    ang = phantom.angles_deg(nang)
+    ofs = O.radon_struct(ang, N, N)
+    img = np.abs(rng.standard_normal((C * Nz, N, N))).astype(np.float32)
+    f = phantom.poisson(O.radon(img, ofs, N), 200.0, seed) + 0.01
+    return N, Nz, C, ang, ofs, f
+
+
+@pytest.mark.parametrize("disc,w", [("KL", 7.0), ("L2", 0.3), ("KL", 1.0)])
+def test_primal_weight_matches_oracle_with_the_same_steps(disc, w):
+    from graptor_gb300.solver import Problem
+    from oracle import oracle as O
+    N, Nz, C, ang, ofs, f = _case(disc)
+    mu, ne, iters = [0.3, 0.05], 17.0, 30
+    with Problem(3, N, Nz, C, N, ang, (4.0, 1.0), mu, disc, "TGV", "FROB", 1.0, ne) as p:
+        p.set_data(f).set_primal_weight(w).run(iters).synchronize()
+        assert p.primal_weight == w
+        got = {k: p.get(k) for k in ("u", "lambda", "v", "p")}
+    o = O.Solver(3, N, Nz, C, N, ofs, f, (4.0, 1.0), mu, ne, O.KL if disc == "KL" else O.L2, O.TGV, O.FROB)
+    sig = 1.0 / np.sqrt(17.0) * w
+    o.sc["sigma"], o.sc["tau"] = np.float32(sig), np.float32(1.0 / (np.sqrt(17.0) * w))
+    o.sc["sigma_data"] = np.float32(sig / ne)
+    m = np.asarray(mu, np.float64)
+    o.sc["mu_eff"] = (m if disc == "KL" else m / (sig + m)).astype(np.float32)
+    o.run(iters)
+    for k, ref in (("u", o.u), ("lambda", o.lam), ("v", o.v), ("p", o.p)):
+        assert rel(got[k], ref) <= 1e-5, (k, rel(got[k], ref))
+
+
+def test_primal_weight_one_is_the_reference_pair():
+    from graptor_gb300.solver import Problem
+    N, Nz, C, ang, ofs, f = _case("KL", 5)
+    out = []
+    for weights in ((), (3.0, 1.0)):
+        with Problem(3, N, Nz, C, N, ang, (4.0, 1.0), [0.3, 0.05], normest=17.0) as p:
+            p.set_data(f)
+            for w in weights:
+                p.set_primal_weight(w)
+            p.run(12).synchronize()
+            out.append(p.get("u"))
+    np.testing.assert_array_equal(out[0], out[1])
+
+
+def test_restart_snapshot_and_movement():
+    from graptor_gb300 import GraptorError
+    from graptor_gb300.solver import Problem
+    N, Nz, C, ang, ofs, f = _case("KL", 7)
+    with Problem(3, N, Nz, C, N, ang, (4.0, 1.0), [0.3, 0.05], normest=17.0) as p:
+        p.set_data(f)
+        with pytest.raises(GraptorError):
+            p.movement()  # no snapshot yet
+        with pytest.raises(ValueError):
+            p.set_primal_weight(0.0)
+        p.run(10).synchronize()
+        p.snapshot()
+        assert p.movement() == (0.0, 0.0)
+        before = {k: p.get(k).astype(np.float64) for k in ("u", "p", "v", "w", "lambda")}
+        p.run(7).synchronize()
+        after = {k: p.get(k).astype(np.float64) for k in before}
+        dx = np.sqrt(sum(((after[k] - before[k]) ** 2).sum() for k in ("u", "p")))
+        dy = np.sqrt(sum(((after[k] - before[k]) ** 2).sum() for k in ("v", "w", "lambda")))
+        mx, my = p.movement()
+        assert abs(mx - dx) <= 1e-9 * max(dx, 1e-30) + 1e-12 and abs(my - dy) <= 1e-9 * max(dy, 1e-30) + 1e-12
+        p.restart().synchronize()
+        np.testing.assert_array_equal(p.get("ubar"), p.get("u"))
+        np.testing.assert_array_equal(p.get("pbar"), p.get("p"))
