@@ -341,6 +341,13 @@ def run_ours(args, rank, world, local):
            "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
            "seconds": e2e_s, "includes": "problem setup, H2D of the sinograms, FP64 operator-norm estimate, "
                                          "K iterations, D2H of Solution and Sinogram (one call)"}
+    # time to relative gap: cold plain solver vs learned warm start + batch (the
+    # metric's first quantity), at the tolerance both reach in bounded time (every rank)
+    ttg = None
+    if args.ttg_seeds > 0:
+        ttg = time_to_gap_compare(rank, world, local, args.ttg_seeds)
+        ttg["note"] = ("relative gap 1e-4 is not reached by either arm within 1.2e5 iterations on these problems "
+                       "(the gap stalls near 4e-4 to 7e-4), so the comparison is at the tolerance shown")
     if rank != 0:
         return None
     out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -357,20 +364,29 @@ def run_ours(args, rank, world, local):
            "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline()
+    if ttg is not None:
+        out["time_to_gap"] = ttg
     return out
 
 
-def batched_specs(n=64, seed=0):
-    """64 independent problems: N ~ U{96..512}, angles ~ U{30..180} over [-75, 75] deg,
-    channels ~ U{1..4}, slices ~ U{1..64}, alternating KL / L2, TGV with Frobenius coupling."""
+BATCH_SIZES = {"uneven": dict(N=(96, 512), nang=(30, 180), Nz=(1, 64)),   # the 64-problem batch (config 3)
+               "small": dict(N=(32, 128), nang=(30, 90), Nz=(1, 8))}     # many small problems
+
+
+def batched_specs(n=64, seed=0, sizes="uneven"):
+    """n independent problems: N, angles (over [-75, 75] deg) and slices uniform over
+    the ranges of BATCH_SIZES[sizes] ("uneven": N U{96..512}, angles U{30..180},
+    slices U{1..64}; "small": N U{32..128}, angles U{30..90}, slices U{1..8}),
+    channels U{1..4}, alternating KL / L2, TGV with Frobenius coupling."""
     from graptor_gb300 import phantom
     rng = np.random.default_rng(seed)
+    rg = BATCH_SIZES[sizes]
     specs = []
     for k in range(n):
-        N = int(rng.integers(96, 513))
-        nang = int(rng.integers(30, 181))
+        N = int(rng.integers(rg["N"][0], rg["N"][1] + 1))
+        nang = int(rng.integers(rg["nang"][0], rg["nang"][1] + 1))
         C = int(rng.integers(1, 5))
-        Nz = int(rng.integers(1, 65))
+        Nz = int(rng.integers(rg["Nz"][0], rg["Nz"][1] + 1))
         disc = "KL" if k % 2 == 0 else "L2"
         mu = [0.2] + [0.05] * (C - 1)
         specs.append(dict(dim=3, N=N, Nz=Nz, C=C, nd=N, angles=phantom.angles_deg(nang, -75, 75), alpha=(4.0, 1.0),
@@ -397,21 +413,32 @@ def batched_data(spec, seed):
 
 
 def run_batched(args, rank, world, local):
-    """Config-3 workload: every rank advances its own batch of 64 problems."""
+    """Config-3 workload (or --batch-sizes small): every rank advances its own batch
+    of independent problems, timed four ways: a graph of the members' own tuned
+    iterations on concurrent chains, the same with one fixed launch shape, the
+    fused mode (one launch per phase over every member's work units, fixed shapes),
+    and the problems one after another.  The autotuner's share is its set-up time
+    (gt_set_data with tuning minus without) against the tuned batch's run."""
     import torch
 
     from graptor_gb300.solver import Batch, Problem
     torch.cuda.set_device(local)
-    specs = batched_specs(args.batch, seed=rank)
+    specs = batched_specs(args.batch, seed=rank, sizes=args.batch_sizes)
     datas = [batched_data(sp, k) for k, sp in enumerate(specs)]
     V = sum(sp["N"] ** 2 * sp["Nz"] * sp["C"] for sp in specs)
     out = {}
-    for label, tune in (("autotuned", True), ("fixed_shape", False)):
+    setup_s = {}
+    for label, tune, mode in (("autotuned", True, 0), ("fixed_shape", False, 0), ("fused", False, 1)):
         with Batch([{**sp, "autotune": tune} for sp in specs], device=local) as b:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
             for k in range(len(b)):
                 b[k].set_data(datas[k])
+            torch.cuda.synchronize()
+            setup_s[label] = time.perf_counter() - t0
+            b.set_mode(mode)
             chains_s = {}
-            for chains in ((1, 2, 4, 8, 64) if tune else (8,)):
+            for chains in (((1, 2, 4, 8, 64) if tune else (8,)) if mode == 0 else (1,)):
                 b.set_concurrency(chains)
                 b.run(args.warmup).synchronize()
                 barrier(world)
@@ -422,7 +449,7 @@ def run_batched(args, rank, world, local):
             dt = chains_s[best]
             out[label] = {"seconds": dt, "voxel_iter_per_s": world * V * args.steps / dt, "chains": best,
                           "seconds_by_chains": chains_s, "shapes": [b[k].tuning for k in range(len(b))][:8]}
-    # the same problems one after another (each alone on the GPU)
+    # the same problems one after another (each alone on the GPU, tuned shapes)
     seq = 0.0
     for k, sp in enumerate(specs):
         with Problem(**sp, device=local) as p:
@@ -432,20 +459,27 @@ def run_batched(args, rank, world, local):
             seq += time.perf_counter() - t0
     seq = max_over_ranks(seq, world)
     out["sequential"] = {"seconds": seq, "voxel_iter_per_s": world * V * args.steps / seq}
+    tuning_s = max(0.0, setup_s["autotuned"] - setup_s["fixed_shape"])
+    out["tuning"] = {"seconds": tuning_s, "share_of_tuned_batch": tuning_s / (tuning_s + out["autotuned"]["seconds"]),
+                     "setup_seconds": setup_s}
     if rank != 0:
         return None
-    best = out["autotuned"]
+    best_label = min(("autotuned", "fixed_shape", "fused"), key=lambda k: out[k]["seconds"])
+    best = out[best_label]
+    rg = BATCH_SIZES[args.batch_sizes]
     return {"metric": METRIC, "value": best["voxel_iter_per_s"], "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * best["seconds"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded 10-ellipse phantoms, Poisson peak 1e3)",
-            "config": {"workload": f"batched: {args.batch} independent 3D FROB TGV problems, N U{{96..512}}, "
-                                   "angles U{30..180} over [-75,75] deg, C U{1..4}, Nz U{1..64}, KL/L2 alternating",
+            "config": {"workload": f"batched: {args.batch} independent 3D FROB TGV problems, N U{{{rg['N'][0]}.."
+                                   f"{rg['N'][1]}}}, angles U{{{rg['nang'][0]}..{rg['nang'][1]}}} over [-75,75] deg, "
+                                   f"C U{{1..4}}, Nz U{{{rg['Nz'][0]}..{rg['Nz'][1]}}}, KL/L2 alternating",
                        "voxel_channels_total": V, "sizes": [(sp["N"], sp["Nz"], sp["C"], len(sp["angles"]),
                                                              sp["discrepancy"]) for sp in specs]},
-            "batch": out,
+            "best": best_label, "batch": out,
             "speedup_vs_sequential": out["sequential"]["seconds"] / best["seconds"],
-            "speedup_vs_fixed_shape": out["fixed_shape"]["seconds"] / best["seconds"]}
+            "speedup_fused_vs_graph": out["autotuned"]["seconds"] / out["fused"]["seconds"],
+            "speedup_tuned_vs_fixed_shape": out["fixed_shape"]["seconds"] / out["autotuned"]["seconds"]}
 
 
 WARM = dict(N=128, Nz=32, C=2, nang=71, pre=500, tol=1e-2, check_every=100, max_iters=40000, fallback_after=10000,
@@ -560,17 +594,17 @@ def run_subsample(args, rank, world, local):
                        "voxel_channels_fine_grid": V}}
 
 
-def run_warmstart(args, rank, world, local):
+def time_to_gap_compare(rank, world, local, nseeds, weights=None, N=None, Nz=None, tol=None, fields=("u",)):
     """Time to relative primal-dual gap <= tol on held-out seeded problems
-    (3-D TGV-KL, FROB, 2 channels, 128^2 x 32 unless --n / --nz, 71 angles): the plain solver
-    cold-started, problems one after another, against the learned warm start
-    (pre cold iterations, U-Net prediction of u, lambda from K u; at a check
-    that finds a problem's gap infinite, u is lifted along the rays with data
-    it misses; a problem whose gap is still infinite fallback_after iterations
-    after the prediction goes back to its cold iterate) with all problems
-    advanced together as one Batch; converged problems leave the batch.  Set-up (buffers, data upload,
-    operator norm, autotuning) is outside both timed regions; gap checks every
-    check_every iterations are inside both."""
+    (3-D TGV-KL, FROB, 2 channels, 128^2 x 32 unless N / Nz given, 71 angles): the
+    plain solver cold-started, problems one after another, against the learned
+    warm start (pre cold iterations, U-Net prediction of u, lambda from K u; at a
+    check that finds a problem's gap infinite, u is lifted along the rays with data
+    it misses; a problem whose gap is still infinite fallback_after iterations after
+    the prediction goes back to its cold iterate) with all problems advanced
+    together as one Batch; converged problems leave the batch.  Set-up (buffers,
+    data upload, operator norm, autotuning) is outside both timed regions; gap
+    checks every check_every iterations are inside both."""
     import math
 
     import torch
@@ -578,11 +612,13 @@ def run_warmstart(args, rank, world, local):
     from graptor_gb300 import warmstart as WS
     from graptor_gb300.solver import Batch, Problem
     torch.cuda.set_device(local)
-    N, Nz, C, tol = WARM["N"], WARM["Nz"], WARM["C"], WARM["tol"]
-    seeds = [9000 + 1000 * rank + k for k in range(args.seeds)]
+    N, Nz, C = N or WARM["N"], Nz or WARM["Nz"], WARM["C"]
+    tol = tol or WARM["tol"]
+    seeds = [9000 + 1000 * rank + k for k in range(nseeds)]
     cases = [WS.phantom_case(s, N, Nz, C, WARM["nang"], device=local) for s in seeds]
     specs = [WS.problem_spec(N, Nz, C, ang) for _, ang in cases]
-    net = WS.UNet3D.load(args.weights or WARM["weights"], device=local)
+    wpath = weights or WARM["weights"]
+    net = WS.UNet3D.load(wpath, device=local)
 
     def done(g):
         return math.isfinite(g) and g <= tol
@@ -608,7 +644,7 @@ def run_warmstart(args, rank, world, local):
         barrier(world)
         t0 = time.perf_counter()
         b.run(WARM["pre"]).synchronize()
-        ws = WS.WarmStarter(net, ("u",), pre_iters=0)
+        ws = WS.WarmStarter(net, tuple(fields), pre_iters=0)
         snaps = [ws.apply(b[k], f, keep_snapshot=True) for k, (f, _) in enumerate(cases)]
         its = WARM["pre"]
         fell_back = [False] * len(cases)
@@ -632,18 +668,76 @@ def run_warmstart(args, rank, world, local):
         warm_s = time.perf_counter() - t0
     cold_s = max_over_ranks(cold_s, world)
     warm_s = max_over_ranks(warm_s, world)
+    return {"tolerance": tol, "seeds": seeds, "size": [N, N, Nz, C], "cold_seconds": cold_s,
+            "warm_batched_seconds": warm_s, "ratio": cold_s / warm_s, "cold_iterations": cold_its,
+            "warm_iterations": warm_its, "fell_back_to_cold": fell_back, "pre_iterations": WARM["pre"],
+            "check_every": WARM["check_every"], "weights": os.path.relpath(wpath, ROOT), "fields": list(fields),
+            "gpu_launches": lpi * (sum(cold_its) + len(cases) * its)}
+
+
+def run_gapsweep(args, rank, world, local):
+    """Relative primal-dual gap and distance moved against iterations for a list of
+    primal weights (--primal-weights; sigma = w/sqrt(Lsqr), tau = 1/(w sqrt(Lsqr)),
+    w = 1 the reference's pair), cold start, one held-out problem (seed 9000) of
+    the time-to-gap workload (3-D TGV-KL, FROB, 2 channels, 71 angles; --n / --nz);
+    --steps iterations, a record every 5000: gap, its box term U sum min(0, K^T
+    lambda - div v~) (the dual's bound for u in [0, U], U = 2 max u), the primal
+    distance moved relative to ||u|| and the dual distance moved."""
+    import math
+
+    import torch
+
+    from graptor_gb300 import warmstart as WS
+    from graptor_gb300.solver import Problem
+    torch.cuda.set_device(local)
+    N, Nz = args.n or WARM["N"], args.nz or WARM["Nz"]
+    f, ang = WS.phantom_case(9000 + rank, N, Nz, WARM["C"], WARM["nang"], device=local)
+    rows = []
+    for w in [float(x) for x in args.primal_weights.split(",")]:
+        with Problem(**WS.problem_spec(N, Nz, WARM["C"], ang), device=local) as p:
+            p.set_data(f).set_primal_weight(w).snapshot()
+            t0 = time.perf_counter()
+            hist, done = [], 0
+            while done < args.steps:
+                p.run(5000)
+                done += 5000
+                g = p.gap()
+                mx, my = p.movement()
+                un = float(np.linalg.norm(p.get("u")))
+                hist.append({"iterations": done, "relative_gap": g["relative"], "box_term": g["dual"] + g["fstar"],
+                             "gap": g["gap"], "primal_moved_rel": mx / max(un, 1e-30), "dual_moved": my})
+                p.snapshot()
+                if math.isfinite(g["relative"]) and g["relative"] <= 1e-4:
+                    break
+            rows.append({"primal_weight": w, "seconds": time.perf_counter() - t0, "history": hist})
     if rank != 0:
         return None
-    return {"metric": "time-to-gap", "value": warm_s, "unit": "s", "n_gpus": world, "steps": len(cases),
-            "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded 2-channel ellipsoid phantoms, Poisson peaks 1e4 / 20)",
-            "config": {"workload": f"time to relative gap <= {tol}: {len(cases)} held-out 3D TGV-KL FROB problems "
-                                   f"{N}x{N}x{Nz}, {C} channels, {WARM['nang']} angles",
-                       "pre_iterations": WARM["pre"], "check_every": WARM["check_every"],
-                       "weights": os.path.relpath(args.weights or WARM["weights"], ROOT)},
-            "cold_seconds": cold_s, "warm_batched_seconds": warm_s, "speedup": cold_s / warm_s,
-            "cold_iterations": cold_its, "warm_iterations": warm_its, "fell_back_to_cold": fell_back,
-            "gpu_launches": lpi * (sum(cold_its) + len(cases) * its)}
+    best = min(rows, key=lambda r: r["history"][-1]["relative_gap"])
+    return {"metric": "relative-gap", "value": best["history"][-1]["relative_gap"], "unit": "relative gap",
+            "n_gpus": world, "steps": args.steps, "warmup": 0, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 2-channel ellipsoid phantom)",
+            "config": {"workload": f"primal-weight sweep: 3D TGV-KL FROB {N}x{N}x{Nz}, 2 channels, "
+                                   f"{WARM['nang']} angles, cold start"},
+            "sweep": rows}
+
+
+def run_warmstart(args, rank, world, local):
+    """The time-to-gap comparison (time_to_gap_compare) as its own bench line."""
+    r = time_to_gap_compare(rank, world, local, args.seeds, args.weights, args.n, args.nz, args.tol,
+                            tuple(args.fields.split(",")))
+    if rank != 0:
+        return None
+    N, _, Nz, C = r["size"]
+    return {"metric": "time-to-gap", "value": r["warm_batched_seconds"], "unit": "s", "n_gpus": world,
+            "steps": len(r["seeds"]), "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded 2-channel ellipsoid phantoms, Poisson peaks 1e4 / 20)",
+            "config": {"workload": f"time to relative gap <= {r['tolerance']}: {len(r['seeds'])} held-out 3D TGV-KL "
+                                   f"FROB problems {N}x{N}x{Nz}, {C} channels, {WARM['nang']} angles",
+                       "pre_iterations": r["pre_iterations"], "check_every": r["check_every"],
+                       "weights": r["weights"]},
+            "cold_seconds": r["cold_seconds"], "warm_batched_seconds": r["warm_batched_seconds"],
+            "speedup": r["ratio"], "cold_iterations": r["cold_iterations"], "warm_iterations": r["warm_iterations"],
+            "fell_back_to_cold": r["fell_back_to_cold"], "gpu_launches": r["gpu_launches"]}
 
 
 def ncu_traffic(kernel):
@@ -775,13 +869,21 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="image side (default 256); profiler captures")
     ap.add_argument("--nang", type=int, default=None,
                     help="projection angles (default 71; the 768^2 x 384 large run uses 141)")
-    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart", "unet", "subsample", "badproj"],
+    ap.add_argument("--workload", default="coupled3d", choices=["coupled3d", "batched", "warmstart", "gapsweep", "unet", "subsample", "badproj"],
                     help="coupled3d: the 3-D 4-channel workload (default); batched: 64 uneven problems; "
-                         "warmstart: time to gap, cold start against learned warm start + batch; unet: the "
+                         "warmstart: time to gap, cold start against learned warm start + batch; gapsweep: gap "
+                         "against iterations for several primal weights; unet: the "
                          "warm-start network's forward pass; subsample: the two-resolution solver; badproj: "
                          "bad-projection detection on nang projections x N x N")
     ap.add_argument("--batch", type=int, default=64, help="problems per rank for --workload batched")
+    ap.add_argument("--batch-sizes", default="uneven", choices=sorted(BATCH_SIZES),
+                    help="--workload batched: the uneven config-3 sizes or many small problems")
     ap.add_argument("--seeds", type=int, default=8, help="held-out problems per rank for --workload warmstart")
+    ap.add_argument("--primal-weights", default="1,3,10", help="--workload gapsweep: primal weights to sweep")
+    ap.add_argument("--fields", default="u", help="--workload warmstart: the fields the network predicts (u or u,v)")
+    ap.add_argument("--tol", type=float, default=None, help="--workload warmstart: relative gap tolerance (1e-2)")
+    ap.add_argument("--ttg-seeds", type=int, default=4,
+                    help="held-out problems of the time-to-gap object in the default line (0: leave it out)")
     ap.add_argument("--weights", default=None, help="network weights for --workload warmstart")
     ap.add_argument("--coupling", default="FROB", choices=["FROB", "UNCORR", "NUCL"],
                     help="channel coupling of the coupled3d workload (default FROB, the headline)")
@@ -812,6 +914,8 @@ def main():
         out = run_batched(args, rank, world, local)
     elif args.workload == "warmstart":
         out = run_warmstart(args, rank, world, local)
+    elif args.workload == "gapsweep":
+        out = run_gapsweep(args, rank, world, local)
     elif args.workload == "unet":
         out = run_unet(args, rank, world, local)
     elif args.workload == "subsample":

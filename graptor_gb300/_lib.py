@@ -89,6 +89,8 @@ _SIGS = {
     "gt_batch_invalidate": (ctypes.c_int, [_P]),
     "gt_batch_set_concurrency": (ctypes.c_int, [_P, ctypes.c_int]),
     "gt_batch_set_active": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "gt_batch_set_mode": (ctypes.c_int, [_P, _I]),
+    "gt_batch_get_mode": (ctypes.c_int, [_P]),
     "gt_get_state_device": (ctypes.c_int, [_P, ctypes.c_int, _P]),
     "gt_set_state_device": (ctypes.c_int, [_P, ctypes.c_int, _P]),
     "gt_problem_stream": (ctypes.c_void_p, [_P]),

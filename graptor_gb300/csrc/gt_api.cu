@@ -43,6 +43,10 @@ cudaError_t launch_lambda_update(float *lam, const float *ku, const float *f, co
                                  long long n, int S, int Nz, int disc, cudaStream_t st);
 cudaError_t launch_sumsq(const float *x, long long n, double *part, int nb, cudaStream_t st);
 cudaError_t launch_sqdiff(const float *a, const float *b, long long n, double *part, int nb, cudaStream_t st);
+long long batch_blocks(const Dims &d, int ph);
+int batch_shape(const Dims &d);
+cudaError_t launch_batch_phase(const BatchTab &T, int ph, long long blocks, int dim, int tgv, int cpl, int cmax,
+                               cudaStream_t st);
 cudaError_t launch_scale_f32(float *x, long long n, float s, cudaStream_t st);
 cudaError_t launch_add2(float *a, float *b, const float *d, long long n, cudaStream_t st);
 cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, double *d_img, double *d_sino,
@@ -304,7 +308,22 @@ int autotune(gt_problem *p) {
   const int nc[3] = {std::min(kMaxCfg, gt::num_proj_configs(p->d.S, 0)),
                      std::min(kMaxCfg, gt::num_proj_configs(p->d.S, 1)),
                      std::min(kMaxCfg, gt::num_dual_configs(p->P))};
-  auto skipped = [](int which, int c) { return which == 1 && (c == 14 || c == 15); };
+  // Shapes left out of the tuning (all stay selectable by gt_set_tuning), to bound
+  // its time on batches of many distinct problems: the TMA back projector (above);
+  // the multi-bin / multi-pixel run shapes (forward 5-8, back 9-12) once S >= 32,
+  // 2-4x slower than the best shape on every measured workload there; the
+  // chunk-outermost shapes (forward 9, back 13), which only pay when the image
+  // exceeds L2, below 64 MB of image; one slice per thread (forward 4, back 8)
+  // once S >= 128.
+  const int S = p->d.S;
+  const long long img_bytes = (long long)p->d.N * p->d.N * S * 4;
+  auto skipped = [&](int which, int c) {
+    if (which == 1 && (c == 14 || c == 15)) return true;
+    if (S >= 32 && ((which == 0 && c >= 5 && c <= 8) || (which == 1 && c >= 9 && c <= 12))) return true;
+    if (img_bytes < (64ll << 20) && ((which == 0 && c == 9) || (which == 1 && c == 13))) return true;
+    if (S >= 128 && ((which == 0 && c == 4) || (which == 1 && c == 8))) return true;
+    return false;
+  };
   p->P.fwd_cfg = 0;
   p->P.bp_cfg = 0;
   p->P.dual_cfg = 0;
@@ -335,8 +354,8 @@ int autotune(gt_problem *p) {
       for (int c = 0; c < nc[which]; ++c) best_ms = std::min(best_ms, ms_cfg[which][c]);
       for (int c = 0; c < nc[which] && rc == GT_OK; ++c) {
         if (skipped(which, c)) continue;
-        // after the first round only configurations within 30 % of the best are timed again
-        if (round > 0 && ms_cfg[which][c] > 1.3f * best_ms) continue;
+        // after the first round only configurations within 15 % of the best are timed again
+        if (round > 0 && ms_cfg[which][c] > 1.15f * best_ms) continue;
         gt::IterParams Q = p->P;
         if (which == 0) Q.fwd_cfg = c; else if (which == 1) Q.bp_cfg = c; else Q.dual_cfg = c;
         auto launch = [&]() {
@@ -344,15 +363,18 @@ int autotune(gt_problem *p) {
           if (which == 1) return gt::launch_bp(Q, p->stream);
           return gt::launch_dual(Q, tgv, p->cpl, p->stream);
         };
+        // the first round screens every shape with one timed launch, later rounds
+        // time the contenders twice
+        const int reps = round == 0 ? 1 : 2;
         cudaError_t e = launch();  // warm-up
         if (e == cudaSuccess) e = cudaEventRecord(e0, p->stream);
-        for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = launch();
+        for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch();
         if (e == cudaSuccess) e = cudaEventRecord(e1, p->stream);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         float ms = 0.f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
         if (e != cudaSuccess) { rc = cuda_err(e, "autotune", __LINE__); break; }
-        ms_cfg[which][c] = std::min(ms_cfg[which][c], ms / 2);
+        ms_cfg[which][c] = std::min(ms_cfg[which][c], ms / reps);
       }
     }
   }
@@ -375,8 +397,11 @@ int autotune(gt_problem *p) {
   p->P.bp_cfg = best[1];
   p->P.dual_cfg = best[2];
   // the schedule (TGV only: TV has no p / pbar half): graph-captured iterations of
-  // each, the faster kept; concurrency between the kernels decides, not their times alone
-  if (tgv && !p->schedule_set) {
+  // each, the faster kept; concurrency between the kernels decides, not their times
+  // alone.  Problems below 8M voxel-channels keep schedule 1 (the two schedules are
+  // within a few per cent there, e.g. 0.135 / 0.132 ms at 128^2 x 32 x 2).
+  if (tgv && !p->schedule_set && p->d.vol < (8u << 20)) p->schedule = 1;
+  if (tgv && !p->schedule_set && p->d.vol >= (8u << 20)) {
     float ms_s[2] = {1e30f, 1e30f};
     for (int round = 0; round < 2 && rc == GT_OK; ++round) {
       for (int sched = 0; sched < 2 && rc == GT_OK; ++sched) {
@@ -1148,11 +1173,79 @@ struct gt_batch {
   int chains = 8;  // problems are spread over this many concurrent chains
   long long iters = 0;
   std::vector<char> active;  // problems advanced by gt_batch_run
+  int mode = 0;              // 0: a graph of per-problem chains; 1: fused launches over all members
+  void *tab = nullptr;       // mode 1: device tables (members' IterParams, per-phase block starts, data terms)
+  size_t tab_bytes = 0;
 };
 
 // One iteration of every problem: problem k runs on chain k % chains; chains run
 // concurrently, problems of one chain one after another.
+// Fused mode: per phase, one launch over the blocks of every active member.
+// The tables are rebuilt (synchronously, before the capture) from the members'
+// current parameters.
+static int batch_capture_fused(gt_batch *b, int n, cudaGraphExec_t *out) {
+  std::vector<gt_problem *> act;
+  for (size_t k = 0; k < b->probs.size(); ++k)
+    if (b->active[k]) act.push_back(b->probs[k]);
+  const int na = (int)act.size();
+  gt_problem *p0 = act[0];
+  int cmax = 4;
+  for (auto p : act) if (p->d.C > 4) cmax = 8;
+  std::vector<gt::IterParams> P(na);
+  std::vector<int> disc(2 * (size_t)na), start(4 * (size_t)(na + 1));  // data terms, then shapes
+  long long total[4] = {0, 0, 0, 0};
+  for (int ph = 0; ph < 4; ++ph) {
+    for (int k = 0; k < na; ++k) {
+      start[(size_t)ph * (na + 1) + k] = (int)total[ph];
+      total[ph] += gt::batch_blocks(act[k]->d, ph);
+    }
+    start[(size_t)ph * (na + 1) + na] = (int)total[ph];
+    if (total[ph] >= (1ll << 31)) return set_err(GT_ERR_ARG, "fused batch: more than 2^31 blocks in one launch");
+  }
+  for (int k = 0; k < na; ++k) {
+    P[k] = act[k]->P;
+    P[k].cbase = 0;
+    disc[k] = act[k]->disc == GT_KL ? gt::KL : gt::L2;
+    disc[na + k] = gt::batch_shape(act[k]->d);
+  }
+  const size_t offP = 0, offS = align256(sizeof(gt::IterParams) * na), offD = offS + align256(sizeof(int) * start.size());
+  const size_t bytes = offD + sizeof(int) * 2 * na;
+  if (bytes > b->tab_bytes) {
+    if (b->tab) cudaFree(b->tab);
+    b->tab = nullptr;
+    b->tab_bytes = 0;
+    CK(cudaMalloc(&b->tab, bytes));
+    b->tab_bytes = bytes;
+  }
+  char *t = (char *)b->tab;
+  CK(cudaMemcpyAsync(t + offP, P.data(), sizeof(gt::IterParams) * na, cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(t + offS, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(t + offD, disc.data(), sizeof(int) * 2 * na, cudaMemcpyHostToDevice, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  const int tgv = p0->reg == GT_TGV, cpl = p0->cpl == GT_FROB ? gt::FROB : gt::UNCORR;
+  for (int it = 0; it < n && e == cudaSuccess; ++it) {
+    for (int ph = 0; ph < 4 && e == cudaSuccess; ++ph) {
+      gt::BatchTab T{(const gt::IterParams *)(t + offP), (const int *)(t + offS) + (size_t)ph * (na + 1),
+                     (const int *)(t + offD), (const int *)(t + offD) + na, na};
+      e = gt::launch_batch_phase(T, ph, total[ph], p0->d.dim, tgv, cpl, cmax, b->stream);
+    }
+  }
+  cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return cuda_err(e != cudaSuccess ? e : e2, "fused batch capture", __LINE__);
+  }
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_err(e, "cudaGraphInstantiate (fused batch)", __LINE__);
+  return GT_OK;
+}
+
 static int batch_capture(gt_batch *b, int n, cudaGraphExec_t *out) {
+  if (b->mode == 1) return batch_capture_fused(b, n, out);
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   int rc = GT_OK;
@@ -1197,9 +1290,30 @@ void gt_batch_destroy(gt_batch *b) {
   for (auto e : b->joins) if (e) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);
   for (auto p : b->probs) gt_problem_destroy(p);
+  if (b->tab) cudaFree(b->tab);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
+
+int gt_batch_set_mode(gt_batch *b, int mode) {
+  if (!b || (mode != 0 && mode != 1)) return set_err(GT_ERR_ARG, "gt_batch_set_mode: mode must be 0 or 1");
+  if (mode == 1) {
+    const gt_problem *p0 = b->probs[0];
+    for (auto p : b->probs) {
+      if (p->d.dim != p0->d.dim || p->reg != p0->reg || p->cpl != p0->cpl)
+        return set_err(GT_ERR_ARG, "fused batch: every member needs the same dimension, regularisation and coupling");
+      if (p->cpl == GT_NUCL) return set_err(GT_ERR_ARG, "fused batch: nuclear coupling is not supported");
+      if (p->d.C > 8) return set_err(GT_ERR_ARG, "fused batch: at most 8 channels per member");
+      if (p->lsqr > 0) return set_err(GT_ERR_ARG, "fused batch: members of the two-resolution solver are not supported");
+    }
+  }
+  CK(cudaSetDevice(b->device));
+  CK(cudaStreamSynchronize(b->stream));
+  b->mode = mode;
+  return gt_batch_invalidate(b);
+}
+
+int gt_batch_get_mode(const gt_batch *b) { return b ? b->mode : -1; }
 
 int gt_batch_create(int n, const gt_desc *descs, gt_batch **out) {
   if (!descs || !out || n < 1) return set_err(GT_ERR_ARG, "gt_batch_create: need n >= 1 descriptions");

@@ -65,4 +65,15 @@ struct IterParams {
   unsigned bp_wait_limit;  // polls of one bounded wait in k_bp_tma
 };
 
+// Members of a fused batch launch (gt_batch mode 1): one launch covers the work
+// units of every member; block b belongs to the member k with start[k] <= b <
+// start[k + 1] and runs that member's kernel body as its block b - start[k].
+struct BatchTab {
+  const IterParams *P;   // [n] the members' iteration parameters (device copy)
+  const int *start;      // [n + 1] first block of each member in this launch
+  const int *disc;       // [n] data term of each member (KL / L2)
+  const int *shape;      // [n] slices per thread of the member's projector / update bodies: 0 one, 1 four, 2 eight
+  int n;
+};
+
 }  // namespace gt

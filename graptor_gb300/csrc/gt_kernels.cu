@@ -328,11 +328,11 @@ __device__ __forceinline__ void dual_project(const IterParams &P, const int nC, 
 // 2-D :286-304), NormV / NormW (3-D :290-610, 2-D :98-258)
 // thread = one (pixel, z); it owns all C channels of that voxel.
 // ===========================================================================
-template <int DIM, bool TGV, int CPL, int CMAX, int MINB = 1>
-__global__ void __launch_bounds__(256, MINB) k_dual(const IterParams P) {
+template <int DIM, bool TGV, int CPL, int CMAX>
+__device__ __forceinline__ void dual_body(const IterParams &P, long long bid) {
   constexpr int K = DIM, KW = DIM == 3 ? 6 : 3;
   const Dims d = P.d;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long t = bid * blockDim.x + threadIdx.x;
   if (t >= (long long)d.N * d.N * d.Nz) return;
   const int pix = (int)(t / d.Nz);
   const int z = (int)(t - (long long)pix * d.Nz);
@@ -398,6 +398,11 @@ __global__ void __launch_bounds__(256, MINB) k_dual(const IterParams P) {
       for (int k = 0; k < KW; ++k) P.w[k * vol + i] = ww[c][k];
     }
   }
+}
+
+template <int DIM, bool TGV, int CPL, int CMAX, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) k_dual(const IterParams P) {
+  dual_body<DIM, TGV, CPL, CMAX>(P, blockIdx.x);
 }
 
 // k_dual_pf: k_dual for a launch whose channel count is exactly CN (no channel
@@ -1069,8 +1074,8 @@ struct Slices {
 // Map a thread to (unit, slice set).  VW = 8: one warp per (unit, 256-slice block);
 // otherwise one thread per (unit, VW slices).  Returns false past the end.
 template <int VW>
-__device__ __forceinline__ bool map_thread(long long units, int S, long long &unit, Slices<VW> &sl) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ bool map_thread(long long bid, long long units, int S, long long &unit, Slices<VW> &sl) {
+  const long long t = bid * blockDim.x + threadIdx.x;
   if (VW == 8 || VW == 4) {
     const int span = VW * 32;
     const int nblk = (S + span - 1) / span;
@@ -1089,6 +1094,11 @@ __device__ __forceinline__ bool map_thread(long long units, int S, long long &un
     sl.va = sl.vb = true;
   }
   return true;
+}
+
+template <int VW>
+__device__ __forceinline__ bool map_thread(long long units, int S, long long &unit, Slices<VW> &sl) {
+  return map_thread<VW>((long long)blockIdx.x, units, S, unit, sl);
 }
 
 template <int VW>
@@ -1340,8 +1350,8 @@ __device__ __forceinline__ void radon_table(const float *__restrict__ img, size_
 }
 
 // k_fwd: radon of ubar fused with update_lambda_KL (3-D :690-704) or _L2 (:677-688).
-template <int DISC, int VW, int UNR, bool WL = false, int MINB = 1>
-__global__ void __launch_bounds__(256, MINB) k_fwd(const IterParams P) {
+template <int DISC, int VW, int UNR, bool WL = false>
+__device__ __forceinline__ void fwd_body(const IterParams &P, long long bid) {
   const Dims d = P.d;
   long long unit;
   typename std::conditional<WL, SlicesWL, Slices<VW>>::type sl;
@@ -1349,7 +1359,7 @@ __global__ void __launch_bounds__(256, MINB) k_fwd(const IterParams P) {
     static_assert(VW == 1, "one slice per lane");
     if (!map_thread_wl((long long)d.nd * d.nang, d.S, unit, sl)) return;
   } else {
-    if (!map_thread<VW>((long long)d.nd * d.nang, d.S, unit, sl)) return;
+    if (!map_thread<VW>(bid, (long long)d.nd * d.nang, d.S, unit, sl)) return;
   }
   const int b = (int)unit;
   const int j = b / d.nd, i = b - j * d.nd;
@@ -1381,6 +1391,11 @@ __global__ void __launch_bounds__(256, MINB) k_fwd(const IterParams P) {
     }
   }
   sl.store(P.lam + q, lam);
+}
+
+template <int DISC, int VW, int UNR, bool WL = false, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) k_fwd(const IterParams P) {
+  fwd_body<DISC, VW, UNR, WL>(P, blockIdx.x);
 }
 
 // ===========================================================================
@@ -1736,7 +1751,7 @@ __global__ void __launch_bounds__(256) k_bp_run(const IterParams P) {
 // k_bp: back projection K* lambda of every (pixel, slice) into P.kstar; it only
 // needs lambda, so it runs beside k_dual.
 template <int VW, int AU, bool TAB, bool WL = false, int UA = 2>
-__global__ void __launch_bounds__(256) k_bp(const IterParams P) {
+__device__ __forceinline__ void bp_body(const IterParams &P, long long bid) {
   const Dims d = P.d;
   long long unit;
   typename std::conditional<WL, SlicesWL, Slices<VW>>::type sl;
@@ -1744,7 +1759,7 @@ __global__ void __launch_bounds__(256) k_bp(const IterParams P) {
     static_assert(VW == 1 && !TAB, "one slice per lane, geometry on the fly");
     if (!map_thread_wl((long long)d.N * d.N, d.S, unit, sl)) return;
   } else {
-    if (!map_thread<VW>((long long)d.N * d.N, d.S, unit, sl)) return;
+    if (!map_thread<VW>(bid, (long long)d.N * d.N, d.S, unit, sl)) return;
   }
   const int pix = (int)unit;
   float acc[VW];
@@ -1755,6 +1770,11 @@ __global__ void __launch_bounds__(256) k_bp(const IterParams P) {
     radon_ad_pixel<VW, false, AU, decltype(sl), UA>(P.lam, d.S, d.nd, d.nang, P.ofs, (float)x, (float)y, sl, acc);
   }
   sl.store(P.kstar + (size_t)pix * d.S, acc);
+}
+
+template <int VW, int AU, bool TAB, bool WL = false, int UA = 2>
+__global__ void __launch_bounds__(256) k_bp(const IterParams P) {
+  bp_body<VW, AU, TAB, WL, UA>(P, blockIdx.x);
 }
 
 // k_bp_tma: back projection with the sinogram rows a pixel tile needs staged in
@@ -1922,10 +1942,10 @@ cudaError_t prepare_bp_tma() {
 // k_update: update_u + update_p + extrapolation for UW consecutive slices (PART:
 // both halves, or one of them, see primal_update).
 template <int DIM, bool TGV, int UW, int PART = PART_ALL>
-__global__ void __launch_bounds__(256) k_update(const IterParams P) {
+__device__ __forceinline__ void update_body(const IterParams &P, long long bid) {
   const Dims d = P.d;
   const int nsg = d.S / UW;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long t = bid * blockDim.x + threadIdx.x;
   if (t >= (long long)d.N * d.N * nsg) return;
   const int pix = (int)(t / nsg);
   const int s0 = (int)(t - (long long)pix * nsg) * UW;
@@ -1933,6 +1953,11 @@ __global__ void __launch_bounds__(256) k_update(const IterParams P) {
   float ks[UW];
   if (PART != PART_P) ldw<UW>(P.kstar + (size_t)pix * d.S + s0, ks);
   primal_update<DIM, TGV, UW, PART>(P, x, y, s0, ks);
+}
+
+template <int DIM, bool TGV, int UW, int PART = PART_ALL>
+__global__ void __launch_bounds__(256) k_update(const IterParams P) {
+  update_body<DIM, TGV, UW, PART>(P, blockIdx.x);
 }
 
 // ===========================================================================
@@ -2957,6 +2982,131 @@ cudaError_t launch_bp(const IterParams &P, cudaStream_t st) {
     bp_vw<2, 2>(P, st);
   } else {
     bp_vw<1, 2>(P, st);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// fused batch launches: the work units of every member in one launch per phase.
+// Every member runs the same kernel body as in its own launch with a shape fixed
+// by its slice count (batch_shape: dual k_dual, thread per voxel with all
+// channels; forward the ray table; back projection geometry on the fly; update
+// 4, 2 or 1 slices per thread as launch_update), so the iterates are identical to
+// solving each member alone (all launch shapes give identical iterates).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int batch_member(const int *__restrict__ start, int n, long long b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(start + mid) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int DIM, bool TGV, int CPL, int CMAX>
+__global__ void __launch_bounds__(256) k_dual_batch(const BatchTab T) {
+  const int k = batch_member(T.start, T.n, blockIdx.x);
+  const IterParams P = T.P[k];
+  dual_body<DIM, TGV, CPL, CMAX>(P, (long long)blockIdx.x - __ldg(T.start + k));
+}
+
+__global__ void __launch_bounds__(256) k_fwd_batch(const BatchTab T) {
+  const int k = batch_member(T.start, T.n, blockIdx.x);
+  const IterParams P = T.P[k];
+  const long long bid = (long long)blockIdx.x - __ldg(T.start + k);
+  const int sh = __ldg(T.shape + k);
+  if (__ldg(T.disc + k) == KL) {
+    if (sh == 2) fwd_body<KL, 8, 4>(P, bid);
+    else if (sh == 1) fwd_body<KL, 4, 4>(P, bid);
+    else fwd_body<KL, 1, 4>(P, bid);
+  } else {
+    if (sh == 2) fwd_body<L2, 8, 4>(P, bid);
+    else if (sh == 1) fwd_body<L2, 4, 4>(P, bid);
+    else fwd_body<L2, 1, 4>(P, bid);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_bp_batch(const BatchTab T) {
+  const int k = batch_member(T.start, T.n, blockIdx.x);
+  const IterParams P = T.P[k];
+  const long long bid = (long long)blockIdx.x - __ldg(T.start + k);
+  const int sh = __ldg(T.shape + k);
+  if (sh == 2) bp_body<8, 1, false, false, 1>(P, bid);
+  else if (sh == 1) bp_body<4, 1, false, false, 1>(P, bid);
+  else bp_body<1, 1, false>(P, bid);
+}
+
+template <int DIM, bool TGV>
+__global__ void __launch_bounds__(256) k_update_batch(const BatchTab T) {
+  const int k = batch_member(T.start, T.n, blockIdx.x);
+  const IterParams P = T.P[k];
+  const long long bid = (long long)blockIdx.x - __ldg(T.start + k);
+  if (P.d.S % 4 == 0) update_body<DIM, TGV, 4, PART_ALL>(P, bid);
+  else if (P.d.S % 2 == 0) update_body<DIM, TGV, 2, PART_ALL>(P, bid);
+  else update_body<DIM, TGV, 1, PART_ALL>(P, bid);
+}
+
+// slices per thread of a member's projector bodies in a fused batch: eight (two
+// float4 chunks 128 apart) for S >= 192, four for 64 <= S < 192, else one (S a
+// multiple of 4 for the vector shapes; small S keeps every lane busy with one)
+int batch_shape(const Dims &d) {
+  if (d.S % 4 != 0 || d.S < 64) return 0;
+  return d.S >= 192 ? 2 : 1;
+}
+
+// blocks of one member in phase ph (0 dual, 1 forward, 2 back projection, 3 update)
+long long batch_blocks(const Dims &d, int ph) {
+  const int sh = batch_shape(d);
+  auto proj = [&](long long units) {
+    return blocks_for(sh == 2 ? threads_for<8>(units, d.S) : sh == 1 ? threads_for<4>(units, d.S)
+                                                                     : threads_for<1>(units, d.S), 256);
+  };
+  switch (ph) {
+    case 0: return blocks_for((long long)d.N * d.N * d.Nz, 256);
+    case 1: return proj((long long)d.nd * d.nang);
+    case 2: return proj((long long)d.N * d.N);
+    default: {
+      const int uw = d.S % 4 == 0 ? 4 : (d.S % 2 == 0 ? 2 : 1);
+      return blocks_for((long long)d.N * d.N * (d.S / uw), 256);
+    }
+  }
+}
+
+// one phase of a fused batch iteration over `blocks` blocks; cmax = 4 or 8 (the
+// dual kernel's channel registers, >= every member's C)
+cudaError_t launch_batch_phase(const BatchTab &T, int ph, long long blocks, int dim, int tgv, int cpl, int cmax,
+                               cudaStream_t st) {
+  if (blocks <= 0) return cudaSuccess;
+  const unsigned g = (unsigned)blocks;
+  switch (ph) {
+    case 0:
+#define GT_DB(D, TG, CP, CM) k_dual_batch<D, TG, CP, CM><<<g, 256, 0, st>>>(T)
+      if (dim == 3) {
+        if (tgv) {
+          if (cpl == FROB) { if (cmax == 4) GT_DB(3, true, FROB, 4); else GT_DB(3, true, FROB, 8); }
+          else { if (cmax == 4) GT_DB(3, true, UNCORR, 4); else GT_DB(3, true, UNCORR, 8); }
+        } else {
+          if (cpl == FROB) { if (cmax == 4) GT_DB(3, false, FROB, 4); else GT_DB(3, false, FROB, 8); }
+          else { if (cmax == 4) GT_DB(3, false, UNCORR, 4); else GT_DB(3, false, UNCORR, 8); }
+        }
+      } else {
+        if (tgv) {
+          if (cpl == FROB) { if (cmax == 4) GT_DB(2, true, FROB, 4); else GT_DB(2, true, FROB, 8); }
+          else { if (cmax == 4) GT_DB(2, true, UNCORR, 4); else GT_DB(2, true, UNCORR, 8); }
+        } else {
+          if (cpl == FROB) { if (cmax == 4) GT_DB(2, false, FROB, 4); else GT_DB(2, false, FROB, 8); }
+          else { if (cmax == 4) GT_DB(2, false, UNCORR, 4); else GT_DB(2, false, UNCORR, 8); }
+        }
+      }
+#undef GT_DB
+      break;
+    case 1: k_fwd_batch<<<g, 256, 0, st>>>(T); break;
+    case 2: k_bp_batch<<<g, 256, 0, st>>>(T); break;
+    default:
+      if (dim == 3) { if (tgv) k_update_batch<3, true><<<g, 256, 0, st>>>(T); else k_update_batch<3, false><<<g, 256, 0, st>>>(T); }
+      else { if (tgv) k_update_batch<2, true><<<g, 256, 0, st>>>(T); else k_update_batch<2, false><<<g, 256, 0, st>>>(T); }
+      break;
   }
   return cudaGetLastError();
 }

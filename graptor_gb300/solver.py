@@ -311,6 +311,17 @@ class Batch:
         L.check(L.lib().gt_batch_set_active(self._b, int(k), int(bool(active))))
         return self
 
+    def set_mode(self, mode: int):
+        """0: a graph of the members' own iterations on concurrent chains (default);
+        1: fused launches, each over the work units of every active member
+        (see gt_batch_set_mode)."""
+        L.check(L.lib().gt_batch_set_mode(self._b, int(mode)))
+        return self
+
+    @property
+    def mode(self) -> int:
+        return int(L.lib().gt_batch_get_mode(self._b))
+
     def set_concurrency(self, chains: int):
         """Spread the problems over `chains` concurrent chains (default 8)."""
         L.check(L.lib().gt_batch_set_concurrency(self._b, int(chains)))

@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
 import time
 
 import numpy as np
@@ -633,19 +634,36 @@ def _main(argv=None):
     ap.add_argument("--eval-seeds", type=int, default=8, help="held-out seeds (seeds 9000..)")
     ap.add_argument("--tol", type=float, default=1e-2)
     ap.add_argument("--json", default=None)
+    ap.add_argument("--pairs-file", default=None, help="npz cache of the training pairs (read if present, else written)")
     a = ap.parse_args(argv)
     fields = tuple(a.fields.split(","))
     log = lambda m: print(m, flush=True)
     out = {}
     if a.command == "train":
         seeds = list(range(1000, 1000 + a.pairs))
-        xs, ys = [], []
-        for k in range(0, len(seeds), 16):
-            x, y = generate_pairs(seeds[k:k + 16], a.N, a.Nz, a.C, a.nang, fields=fields, pre_iters=a.pre_iters,
-                                  target_iters=a.target_iters, log=log)
-            xs.append(x)
-            ys.append(y)
-        xs, ys = np.concatenate(xs), np.concatenate(ys)
+        # pairs are generated with u and v (the union of the fields a network may
+        # predict) and can be cached in --pairs-file for several trainings
+        gen_fields = ("u", "v")
+        if a.pairs_file and os.path.exists(a.pairs_file):
+            z = np.load(a.pairs_file)
+            xs, ys = z["x"], z["y"]
+            log(f"loaded {len(xs)} pairs from {a.pairs_file}")
+        else:
+            xs, ys = [], []
+            for k in range(0, len(seeds), 16):
+                x, y = generate_pairs(seeds[k:k + 16], a.N, a.Nz, a.C, a.nang, fields=gen_fields,
+                                      pre_iters=a.pre_iters, target_iters=a.target_iters, log=log)
+                xs.append(x)
+                ys.append(y)
+            xs, ys = np.concatenate(xs), np.concatenate(ys)
+            if a.pairs_file:
+                np.savez(a.pairs_file, x=xs, y=ys)
+        # the channels of the requested fields, in generate_pairs' order (field-major)
+        offs, o = {}, 0
+        for fl in gen_fields:
+            offs[fl] = o
+            o += FIELD_COMPS[fl] * a.C
+        ys = np.concatenate([ys[:, offs[fl]:offs[fl] + FIELD_COMPS[fl] * a.C] for fl in fields], 1)
         net = UNet3D(a.C, output_channels(a.C, fields), residual=a.C)
         log(f"U-Net parameters: {net.nparams}")
         hist = train(net, xs, ys, steps=a.steps, batch=a.batch, crop=tuple(int(c) for c in a.crop.split(",")),

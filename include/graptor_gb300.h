@@ -231,6 +231,17 @@ GT_API int gt_batch_set_concurrency(gt_batch *b, int chains);
  * gt_batch_run calls, e.g. once it has reached its gap tolerance; its state is
  * kept.  All problems are active after gt_batch_create. */
 GT_API int gt_batch_set_active(gt_batch *b, int k, int active);
+/* How gt_batch_run advances the batch.  Mode 0 (default): one graph of the
+ * members' own iterations (their tuned launch shapes and schedules) on
+ * concurrent chains.  Mode 1 (fused): per iteration four launches, each over the
+ * work units of every active member (dual update, forward projection + data
+ * prox, back projection, primal update), every member with one fixed launch
+ * shape; for many small problems, where per-member launches leave the GPU
+ * underfilled.  Mode 1 needs every member to share the dimension, the
+ * regularisation and the coupling (Frobenius or uncorrelated, <= 8 channels);
+ * it returns GT_ERR_ARG otherwise.  Iterates are identical in both modes. */
+GT_API int gt_batch_set_mode(gt_batch *b, int mode);
+GT_API int gt_batch_get_mode(const gt_batch *b);
 
 /* Kernels of the learned warm start (a small 3-D U-Net whose output initialises
  * the solver's image).  No counterpart in the reference, which always starts

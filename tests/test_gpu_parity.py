@@ -483,3 +483,43 @@ def test_bounded_wait_of_tma_back_projection_reports_timeout():
         p.set_tuning(0, 4)
         p.set_data(f).run(4).synchronize()
         np.testing.assert_array_equal(got, p.get("u"))
+
+
+def test_fused_batch_matches_individual_problems():
+    """The fused batch mode (one launch per phase over every member's work
+    units) gives each member the result it gets alone: uneven sizes, channel
+    counts (S odd, even, a multiple of 4; one, four and eight slices per thread),
+    angle sets and KL/L2, members paused
+    and resumed.  Mixed couplings are refused."""
+    from graptor_gb300 import phantom
+    from graptor_gb300.solver import Batch, Problem
+    rng = np.random.default_rng(23)
+    specs, datas = [], []
+    for k, (N, Nz, C, nang, disc) in enumerate([(24, 5, 2, 20, "KL"), (17, 3, 1, 13, "L2"), (30, 4, 3, 25, "KL"),
+                                                (20, 6, 4, 30, "L2"), (9, 1, 1, 7, "KL"), (41, 2, 2, 33, "L2"),
+                                                (19, 24, 4, 11, "KL"), (13, 50, 4, 9, "L2"), (16, 17, 3, 12, "KL")]):
+        ang = phantom.angles_deg(nang, -75, 75)
+        specs.append(dict(dim=3, N=N, Nz=Nz, C=C, nd=N, angles=ang, alpha=(4.0, 1.0), mu=rng.uniform(0.1, 0.4, C),
+                          discrepancy=disc, regularisation="TGV", coupling="FROB", normest=12.0 + k))
+        datas.append(np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32))
+    with Batch(specs) as b:
+        for k in range(len(b)):
+            b[k].set_data(datas[k])
+        b.set_mode(1)
+        assert b.mode == 1
+        b.run(21)
+        b.set_active(2, False)
+        b.run(9)
+        b.set_active(2, True)
+        b.run(10).synchronize()
+        got = [{f: b[k].get(f) for f in ("u", "lambda", "w")} for k in range(len(b))]
+    for k, sp in enumerate(specs):
+        with Problem(**sp) as p:
+            p.set_data(datas[k]).run(31 if k == 2 else 40).synchronize()
+            for f in got[k]:
+                np.testing.assert_array_equal(got[k][f], p.get(f), err_msg=f"member {k} field {f}")
+    mixed = [dict(specs[0]), dict(specs[1], coupling="UNCORR")]
+    with Batch(mixed) as b:
+        with pytest.raises(ValueError):
+            b.set_mode(1)
+        assert b.mode == 0
