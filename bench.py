@@ -281,6 +281,8 @@ def run_ours(args, rank, world, local):
     if forced:  # launch shapes given on the command line (profiler captures): no tuning launches
         prob.set_tuning(args.fwd_shape or 0, args.bp_shape or 0)
         prob.set_dual_shape(args.dual_shape or 0)
+    if args.schedule is not None:
+        prob.set_schedule(args.schedule)
     prob.run(args.warmup).synchronize()
 
     # ---- device-timed region: K iterations, inputs resident in HBM
@@ -489,8 +491,10 @@ WARM = dict(N=128, Nz=32, C=2, nang=71, pre=500, tol=1e-2, check_every=100, max_
 def run_unet(args, rank, world, local):
     """The warm-start network's forward pass (3-level 3-D U-Net 16-32-64, 2 channels in
     and out, batch 2 of 32x128x128, bfloat16 activations): convolutions with
-    16k input and output channels on the tensor cores (tcgen05), the others on
-    the CUDA cores; the same pass with every convolution on the CUDA cores beside it."""
+    16k input and output channels on the tensor cores (tcgen05; 3x3x3 ones by the
+    kernel that stages input halos and weights in shared memory), the others on
+    the CUDA cores; beside it the same pass with the tensor-core kernel that gathers
+    every tap from global memory, and with every convolution on the CUDA cores."""
     import torch
 
     from graptor_gb300 import _lib as L
@@ -513,7 +517,7 @@ def run_unet(args, rank, world, local):
         if ci % 16 == 0 and co % 16 == 0:
             tc_flops += fl
     times = {}
-    for tc in (0, 1):
+    for tc in (0, 2, 1):  # CUDA cores, tensor cores gathering every tap, tensor cores with staged halos
         L.check(L.lib().gt_nn_set_tensor_cores(tc))
         for _ in range(args.warmup):
             net.forward(x, out)
@@ -541,7 +545,7 @@ def run_unet(args, rank, world, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic",
             "config": {"workload": "warm-start U-Net 16-32-64 forward, batch 2 x 2 channels x 32x128x128",
                        "conv_gflop": flops / 1e9, "tensor_core_gflop": tc_flops / 1e9},
-            "cuda_cores_only_ms": times[0],
+            "cuda_cores_only_ms": times[0], "tensor_cores_gather_ms": times[2],
             "roofline": {"bound": "tensor", "achieved": flops / (ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
                          "frac": flops / (ms / 1e3) / 1e12 / peak, "peak_source": kind, "traffic": None}}
 
@@ -891,6 +895,8 @@ def main():
                     help="force the forward projector's launch shape (no autotuning); profiler captures")
     ap.add_argument("--bp-shape", type=int, default=None, help="force the back projector's launch shape")
     ap.add_argument("--dual-shape", type=int, default=None, help="force the dual kernel's launch shape")
+    ap.add_argument("--schedule", type=int, default=None, choices=[0, 1],
+                    help="force the iteration schedule (0: primal update after the projectors, 1: its p half beside them)")
     ap.add_argument("--quick", action="store_true",
                     help="only the device-timed region (no e2e, kernel timing or CPU baseline): profiler runs")
     args = ap.parse_args()

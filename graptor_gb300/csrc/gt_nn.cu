@@ -256,6 +256,237 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const __nv_bfloat16 *__restri
   if (warp == 0) gt::tmem_dealloc(tmem, ncols);
 }
 
+// ---------------------------------------------------------------------------
+// 3x3x3 forward convolution on the tensor cores with the block's input halo and
+// weights staged once per 16-channel chunk (k_conv3d_tc gathers every tap's
+// operands from global memory).  The weights arrive as one bulk copy per chunk of
+// their shared-memory image (k_conv_wimage, built once per call).  A block owns 128 consecutive voxels of one
+// (b, d) plane: R = 128 / W rows of width W (W <= 128), or 128 voxels of one row
+// (W a multiple of 128).  Per chunk of 16 input channels:
+//   halo     the 3 x (R + 2) x (Wb + 2) input positions the block's 27 taps read,
+//            channels 0-7 and 8-15 as two planes of 16-byte rows (zero outside
+//            the volume);
+//   weights  all 27 taps' Co x 16 weights as 8-row x 16-byte core matrices.
+// A tap's B operand is then a descriptor into the weights.  Its A operand: for
+// W >= 128 the 128 rows are 128 consecutive halo positions, so the descriptor
+// points into the halo itself and the 27 MMAs of a chunk are issued back to back
+// without any copy; for W < 128 the rows of the tap's shifted window are copied
+// from the halo into a double-buffered A tile (two 16-byte shared-memory moves per
+// thread) before each MMA.  Every wait is bounded (g_nn_err on timeout).
+// ---------------------------------------------------------------------------
+constexpr int TC2_A_BYTES = 128 * 16 * 2;
+
+__host__ __device__ inline int tc2_rows(int W) { return W >= 128 ? 1 : 128 / W; }
+__host__ __device__ inline int tc2_width(int W) { return W >= 128 ? 128 : W; }
+__host__ __device__ inline int tc2_halo(int W) { return 3 * (tc2_rows(W) + 2) * (tc2_width(W) + 2); }
+__host__ __device__ inline size_t tc2_align(size_t b) { return (b + 1023) & ~(size_t)1023; }
+// dynamic shared memory: two halo planes, the weights, two A tiles (+ alignment slack)
+inline size_t tc2_smem(int W, int Co) {
+  return tc2_align((size_t)tc2_halo(W) * 32) + tc2_align((size_t)27 * Co * 32) + 2 * TC2_A_BYTES + 1024;
+}
+
+// The weights of every 16-channel chunk as the shared-memory image the MMAs read:
+// per chunk, per tap t, Co rows x 16 channels as 8-row x 16-byte core matrices
+// (tap t at t * Co * 32 bytes, row co at (co / 8) * 256 + (co % 8) * 16, channels
+// 8-15 at + 128).  One thread per 16 bytes.
+__global__ void k_conv_wimage(const __nv_bfloat16 *__restrict__ w, int Ci, int Co, uint4 *__restrict__ img) {
+  const long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long per_chunk = 27ll * Co * 2;
+  if (u >= per_chunk * (Ci / 16)) return;
+  const int ch = (int)(u / per_chunk);
+  const int rem = (int)(u - ch * per_chunk);
+  const int t = rem / (Co * 2), r2 = rem - t * Co * 2;
+  const int cg = r2 >> 4, g = (r2 >> 3) & 1, cr = r2 & 7;  // core-matrix group, channel half, row
+  const int co = cg * 8 + cr;
+  const __nv_bfloat16 *wp = w + ((size_t)co * Ci + ch * 16 + 8 * g) * 27 + t;
+  uint32_t pk[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) pk[j] = bf16_pair(wp[(size_t)(2 * j) * 27], wp[(size_t)(2 * j + 1) * 27]);
+  img[u] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+}
+
+template <class TO>
+__global__ void __launch_bounds__(128) k_conv3d_tc2(const __nv_bfloat16 *__restrict__ x, int Ci, int Cx, int x_off,
+                                                    const uint4 *__restrict__ wimg,
+                                                    const float *__restrict__ bias, TO *__restrict__ y, int Co,
+                                                    int Cy, int co_off, Shape s, int relu, int accumulate) {
+  extern __shared__ uint8_t dsm_raw[];
+  uint8_t *dsm = (uint8_t *)(((uintptr_t)dsm_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t bar[4];  // A stages 0 / 1, chunk completion, weight copy
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int R = tc2_rows(s.W), Wb = tc2_width(s.W), HP = R + 2, WP = Wb + 2;
+  const int P = 3 * HP * WP;
+  const size_t plane_bytes = (size_t)P * 16;
+  uint8_t *sH = dsm;                                   // halo: plane g at sH + g * plane_bytes
+  uint8_t *sW = dsm + tc2_align(plane_bytes * 2);      // weights: tap t at sW + t * Co * 32
+  uint8_t *sA = sW + tc2_align((size_t)27 * Co * 32);  // A tiles (W < 128)
+  const bool direct = s.W >= 128;
+
+  // the block's plane and first row / column
+  const long long v0 = (long long)blockIdx.x * 128;
+  const long long plane_vox = (long long)s.H * s.W;
+  const int bd = (int)(v0 / plane_vox);
+  const int b = bd / s.D, d = bd - b * s.D;
+  const long long in_plane = v0 - (long long)bd * plane_vox;
+  const int h0 = (int)(in_plane / s.W), w0 = (int)(in_plane - (long long)h0 * s.W);
+  const size_t plane = (size_t)s.H * s.W, vol = plane * s.D;
+  // this thread's voxel: row r, column c of the block
+  const int r = direct ? 0 : tid / Wb, c = direct ? tid : tid - (tid / Wb) * Wb;
+
+  const uint32_t ncols = Co <= 32 ? 32u : (Co <= 64 ? 64u : 128u);
+  if (warp == 0) gt::tmem_alloc(&tslot, ncols);
+  if (tid == 0) {
+    gt::mbar_init(&bar[0], 1);
+    gt::mbar_init(&bar[1], 1);
+    gt::mbar_init(&bar[2], 1);
+    gt::mbar_init(&bar[3], 1);
+    gt::mbar_init_fence();
+  }
+  gt::tc_fence_before();
+  __syncthreads();
+  gt::tc_fence_after();
+  const uint32_t tmem = tslot;
+  const uint32_t idesc = gt::tc_idesc_bf16_f32(128, Co);
+  const int nci = Ci / 16;
+  bool ok = true;
+  int q = 0;           // MMAs issued so far (A-tile path: their commits complete the stages in order)
+  int wpending = -1;   // thread 0: parity of a weight copy not yet seen complete
+  for (int ch = 0; ch < nci && ok; ++ch) {
+    const int ci0 = ch * 16;
+    if (ch > 0) {  // every MMA of the previous chunk must be done before its operands are rewritten
+      const bool done = gt::mbar_wait_bounded(&bar[2], (ch - 1) & 1, TC_WAIT_LIMIT);
+      if (__syncthreads_or(!done)) { ok = false; break; }
+    }
+    // weights of the chunk: one bulk copy of its image (only the MMA thread waits for it)
+    const uint32_t wbytes = 27u * Co * 32u;
+    if (tid == 0) {
+      gt::mbar_arrive_expect_tx(&bar[3], wbytes);
+      gt::bulk_load(sW, wimg + (size_t)ch * (wbytes / 16), wbytes, &bar[3]);
+      wpending = ch & 1;
+    }
+    // halo: items of 4 adjacent columns x 16 channels (one 8-byte load per channel;
+    // W and w0 are multiples of 4, so a group is wholly inside or outside the
+    // volume), groups covering columns w0 - 4 .. w0 + Wb + 3, of which the halo keeps
+    // w0 - 1 .. w0 + Wb; zero outside the volume
+    {
+      const __nv_bfloat16 *xc = x + ((size_t)b * Cx + x_off + ci0) * vol;
+      const int ng = Wb / 4 + 2, items = 3 * HP * ng;
+      for (int it = tid; it < items; it += 128) {
+        const int row = it / ng, gq = it - row * ng;
+        const int dd = row / HP, hh = row - dd * HP;
+        const int dg = d - 1 + dd, hg = h0 - 1 + hh, wg4 = w0 - 4 + 4 * gq;
+        uint2 v[16];
+        if (dg >= 0 && dg < s.D && hg >= 0 && hg < s.H && wg4 >= 0 && wg4 < s.W) {
+          const __nv_bfloat16 *xp = xc + (size_t)dg * plane + (size_t)hg * s.W + wg4;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = *reinterpret_cast<const uint2 *>(xp + (size_t)j * vol);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = make_uint2(0u, 0u);
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int ww = 4 * gq - 3 + e;  // halo column of element e (column w0 - 1 is halo column 0)
+          if (ww < 0 || ww >= WP) continue;
+          uint32_t pk[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            // element e of channels 2j and 2j + 1: 16-bit half e & 1 of word e >> 1
+            const uint32_t a = (e >> 1) ? v[2 * j].y : v[2 * j].x, c = (e >> 1) ? v[2 * j + 1].y : v[2 * j + 1].x;
+            pk[j] = (e & 1) ? ((a >> 16) | (c & 0xffff0000u)) : ((a & 0xffffu) | (c << 16));
+          }
+          const size_t pos = (size_t)row * WP + ww;
+          *reinterpret_cast<uint4 *>(sH + pos * 16) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+          *reinterpret_cast<uint4 *>(sH + plane_bytes + pos * 16) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
+      }
+    }
+    gt::fence_async_shared();
+    __syncthreads();
+    if (tid == 0) {
+      if (gt::mbar_wait_bounded(&bar[3], ch & 1, TC_WAIT_LIMIT)) wpending = -1;
+      else ok = false;
+    }
+    if (__syncthreads_or(!ok)) { ok = false; break; }
+    if (direct) {
+      if (tid == 0) {
+        gt::tc_fence_after();
+        for (int t = 0; t < 27; ++t) {
+          const int kd = t / 9, kh = (t / 3) % 3, kw = t % 3;
+          const int p0 = (kd * HP + kh) * WP + kw;
+          gt::tc_mma_bf16(tmem, gt::tc_smem_desc(sH + (size_t)p0 * 16, (uint32_t)plane_bytes, 128),
+                          gt::tc_smem_desc(sW + (size_t)t * Co * 32, 128, 256), idesc, (ch > 0 || t > 0) ? 1 : 0);
+        }
+        gt::tc_commit(&bar[2]);
+      }
+    } else {
+      for (int t = 0; t < 27 && ok; ++t, ++q) {
+        const int st = q & 1;
+        if (q >= 2) {  // the MMA that read this A tile (number q - 2) must have completed
+          const bool done = gt::mbar_wait_bounded(&bar[st], ((q - 2) >> 1) & 1, TC_WAIT_LIMIT);
+          if (__syncthreads_or(!done)) { ok = false; break; }
+        }
+        const int kd = t / 9, kh = (t / 3) % 3, kw = t % 3;
+        const int pos = (kd * HP + r + kh) * WP + c + kw;
+        const uint4 lo = *reinterpret_cast<const uint4 *>(sH + (size_t)pos * 16);
+        const uint4 hi = *reinterpret_cast<const uint4 *>(sH + plane_bytes + (size_t)pos * 16);
+        uint8_t *row = sA + st * TC2_A_BYTES + (tid >> 3) * 256 + (tid & 7) * 16;
+        *reinterpret_cast<uint4 *>(row) = lo;
+        *reinterpret_cast<uint4 *>(row + 128) = hi;
+        gt::fence_async_shared();
+        __syncthreads();
+        if (tid == 0) {
+          gt::tc_fence_after();
+          gt::tc_mma_bf16(tmem, gt::tc_smem_desc(sA + st * TC2_A_BYTES, 128, 256),
+                          gt::tc_smem_desc(sW + (size_t)t * Co * 32, 128, 256), idesc, (ch > 0 || t > 0) ? 1 : 0);
+          gt::tc_commit(&bar[st]);
+          if (t == 26) gt::tc_commit(&bar[2]);  // the chunk's last MMA: its operands may be rewritten after it
+        }
+      }
+    }
+  }
+  // the last chunk's completion covers every MMA
+  if (ok) ok = gt::mbar_wait_bounded(&bar[2], (nci - 1) & 1, TC_WAIT_LIMIT);
+  ok = !__syncthreads_or(!ok);
+  gt::tc_fence_after();
+  const int h = h0 + r, wx = w0 + c;
+  if (ok) {
+    for (int c0 = 0; c0 < Co; c0 += 16) {
+      float v[16];
+      gt::tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      TO *yo = y + ((size_t)b * Cy + co_off + c0) * vol + (size_t)d * plane + (size_t)h * s.W + wx;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        float o = v[k] + (bias ? bias[c0 + k] : 0.f);
+        if (accumulate) o += ld<TO>(yo + (size_t)k * vol);
+        if (relu) o = fmaxf(o, 0.f);
+        st<TO>(yo + (size_t)k * vol, o);
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(&g_nn_err, 1);
+    // a weight copy still in flight lands in this block's shared memory: wait for
+    // it (bounded) before the block ends
+    if (wpending >= 0) gt::mbar_wait_bounded(&bar[3], (uint32_t)wpending, TC_WAIT_LIMIT);
+  }
+  gt::tc_fence_before();
+  __syncthreads();
+  // as in k_conv3d_tc: on the timeout path the block cannot know that the MMA it
+  // waited for has finished when it frees the tensor memory; the error flag makes
+  // the host discard the launch's output
+  if (warp == 0) gt::tmem_dealloc(tmem, ncols);
+}
+
+// the staged kernel applies: 3x3x3, 16k channels in and out, Co <= 128, blocks
+// inside one (b, d) plane and whole rows (or 128-wide row pieces)
+inline bool tc2_ok(int Ci, int Co, const Shape &s) {
+  return Ci % 16 == 0 && Co % 16 == 0 && Co <= 128 && ((long long)s.H * s.W) % 128 == 0 &&
+         (s.W % 128 == 0 || 128 % s.W == 0) && tc2_smem(s.W, Co) <= 227 * 1024;
+}
+
+int g_tc2_mode = 1;  // 1: the staged 3x3x3 tensor-core kernel where it applies
+
 int g_tc_mode = 1;  // 1: tensor-core path where it applies, 0: CUDA cores only
 
 // w[co][ci][t] -> w'[ci][co][K3-1-t]: convolving dY with w' gives dX (stride 1, same padding)
@@ -544,6 +775,36 @@ int gt_nn_conv3d(const void *x, int x_dtype, int Ci, int Cx, int x_off, const vo
   const Shape s{B, D, H, W};
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;
+  if (g_tc_mode && g_tc2_mode && x_dtype == 1 && ksize == 3 && tc2_ok(Ci, Co, s)) {
+    const unsigned g = (unsigned)(((long long)B * D * H * W) / 128);
+    const __nv_bfloat16 *xb = (const __nv_bfloat16 *)x, *wb = (const __nv_bfloat16 *)w_bf16;
+    const size_t smem = tc2_smem(W, Co);
+    // the weights' shared-memory image, in stream-ordered scratch freed after the launch
+    const long long units = 27ll * Co * 2 * (Ci / 16);
+    uint4 *img = nullptr;
+    cudaError_t ea = cudaMallocAsync((void **)&img, sizeof(uint4) * units, st);
+    if (ea == cudaSuccess) {
+      k_conv_wimage<<<(unsigned)((units + 255) / 256), 256, 0, st>>>(wb, Ci, Co, img);
+      ea = cudaGetLastError();
+    }
+    if (ea == cudaSuccess) {
+      if (y_dtype == 1) {
+        ea = cudaFuncSetAttribute(k_conv3d_tc2<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (ea == cudaSuccess)
+          k_conv3d_tc2<__nv_bfloat16><<<g, 128, smem, st>>>(xb, Ci, Cx, x_off, img, bias, (__nv_bfloat16 *)y, Co,
+                                                            Cy, co_off, s, relu, accumulate);
+      } else {
+        ea = cudaFuncSetAttribute(k_conv3d_tc2<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (ea == cudaSuccess)
+          k_conv3d_tc2<float><<<g, 128, smem, st>>>(xb, Ci, Cx, x_off, img, bias, (float *)y, Co, Cy, co_off, s,
+                                                    relu, accumulate);
+      }
+      if (ea == cudaSuccess) ea = cudaGetLastError();
+    }
+    if (img) cudaFreeAsync(img, st);
+    NN_CK(ea, "gt_nn_conv3d (staged tensor-core kernel)");
+    return GT_OK;
+  }
   if (g_tc_mode && x_dtype == 1 && Ci % 16 == 0 && Co % 16 == 0 && Co <= 256) {
     const unsigned g = (unsigned)(((long long)B * D * H * W + 127) / 128);
     const __nv_bfloat16 *xb = (const __nv_bfloat16 *)x, *wb = (const __nv_bfloat16 *)w_bf16;
@@ -573,7 +834,9 @@ int gt_nn_conv3d(const void *x, int x_dtype, int Ci, int Cx, int x_off, const vo
 }
 
 int gt_nn_set_tensor_cores(int on) {
+  if (on < 0 || on > 2) return gt::set_error(GT_ERR_ARG, "gt_nn_set_tensor_cores: 0, 1 or 2");
   g_tc_mode = on ? 1 : 0;
+  g_tc2_mode = on == 1 ? 1 : 0;
   return GT_OK;
 }
 

@@ -277,7 +277,12 @@ GT_API int gt_batch_get_mode(const gt_batch *b);
  * gt_nn_cast: float32 <-> bfloat16 (src_dtype 0: f32 -> bf16, 1: bf16 -> f32).
  * gt_nn_set_tensor_cores: 1 (default) runs gt_nn_conv3d with bfloat16 input,
  *   Ci % 16 == 0, Co % 16 == 0 and Co <= 256 on the tensor cores (tcgen05 MMA, FP32
- *   accumulator in tensor memory), 0 keeps every convolution on the CUDA cores.
+ *   accumulator in tensor memory): 3x3x3 convolutions with Co <= 128 whose
+ *   128-voxel blocks lie in one plane and cover whole rows (H W % 128 == 0 and W
+ *   dividing 128 or a multiple of it) by the kernel that stages each 16-channel
+ *   chunk's input halo and weights in shared memory once, the others by the kernel
+ *   that gathers every tap's operands from global memory; 2 uses the gathering
+ *   kernel for all of them; 0 keeps every convolution on the CUDA cores.
  * gt_nn_check: GT_ERR_TIMEOUT if a tensor-core convolution block gave up a bounded
  *   wait since the last call (its output is then not written; the flag is cleared);
  *   call it after synchronising the stream the convolutions ran on. */

@@ -400,3 +400,46 @@ def test_conv_tensor_cores_match_cuda_cores(k, Ci, Co, ydt):
     # channels outside the view are untouched
     assert torch.equal(outs[1][:, :yoff], y0[:, :yoff].double())
     assert torch.equal(outs[1][:, yoff + Co:], y0[:, yoff + Co:].double())
+
+
+@pytest.mark.parametrize("W,H,Ci,Co,ydt", [(128, 2, 16, 16, 0), (256, 1, 32, 64, 1), (64, 4, 32, 32, 0),
+                                           (32, 4, 16, 64, 0), (16, 8, 48, 16, 1), (8, 16, 16, 32, 0),
+                                           (4, 32, 16, 16, 0)])
+def test_staged_tensor_core_convolution(W, H, Ci, Co, ydt):
+    """The 3x3x3 tensor-core kernel that stages each 16-channel chunk's input halo
+    and weights in shared memory (rows of 128 voxels read straight from the halo for
+    W >= 128, copied into an A tile for W < 128) against the kernel that gathers
+    every tap from global memory, the CUDA cores and float64: channel views, bias,
+    accumulation, ReLU, borders on every side."""
+    L = _lib()
+    lib = L.lib()
+    g = torch.Generator().manual_seed(7 * W + H + Ci + Co)
+    B, D = 2, 3
+    Cx, xoff, Cy, yoff = Ci + 16, 16, Co + 3, 2
+    x = _bf16((B, Cx, D, H, W), g)
+    w = _bf16((Co, Ci, 3, 3, 3), g, 0.1)
+    bias = torch.randn(Co, generator=g)
+    ytype = torch.bfloat16 if ydt else torch.float32
+    y0 = torch.randn((B, Cy, D, H, W), generator=g).to(ytype)
+    outs = {}
+    try:
+        for mode in (0, 2, 1):
+            L.check(lib.gt_nn_set_tensor_cores(mode))
+            y = _d(y0)
+            xd, wd, bd = _d(x), _d(w), _d(bias)
+            L.check(lib.gt_nn_conv3d(_p(xd), 1, Ci, Cx, xoff, _p(wd), _p(bd), _p(y), ydt, Co, Cy, yoff, B, D, H, W, 3,
+                                     1, 1, None))
+            torch.cuda.synchronize()
+            L.check(lib.gt_nn_check())
+            outs[mode] = y.cpu().double()
+    finally:
+        L.check(lib.gt_nn_set_tensor_cores(1))
+    ref = F.conv3d(x[:, xoff:xoff + Ci].double(), w.double(), bias.double(), padding=1)
+    ref = torch.relu(ref + y0[:, yoff:yoff + Co].double())
+    sl = slice(yoff, yoff + Co)
+    tol = 1e-2 if ydt else 1e-5
+    assert rel(outs[1][:, sl], outs[2][:, sl]) < tol
+    assert rel(outs[1][:, sl], outs[0][:, sl]) < tol
+    assert rel(outs[1][:, sl], ref) < tol
+    assert torch.equal(outs[1][:, :yoff], y0[:, :yoff].double())
+    assert torch.equal(outs[1][:, yoff + Co:], y0[:, yoff + Co:].double())
