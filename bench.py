@@ -63,9 +63,14 @@ def algorithmic_bytes(V, Sb):
       launched as two halves (the iteration's schedule):
       k_update_u reads u 4, v 12, K* lambda 4; writes u 4, ubar 4                  (28 B/voxel-ch)
       k_update_p reads p 12, v 12, w 24; writes p 12, pbar 12                      (72 B/voxel-ch)
+    k_dual_fused (schedule 2: the p half of the previous iteration inside the dual kernel)
+             reads ubar 4, p 12, v 12, w 24; writes p 12, v 12, w 24                 (100 B/voxel-ch)
+    The iteration figure stays the unfused one (the algorithm's own traffic); schedule 2
+    moves 100 + 28 + 8 B/voxel-ch + 20 B/bin per iteration.
     """
     return {"iteration": 172 * V + 16 * Sb, "k_dual": 88 * V, "k_fwd": 4 * V + 16 * Sb,
-            "k_bp": 4 * V + 4 * Sb, "k_update": 88 * V, "k_update_u": 28 * V, "k_update_p": 72 * V}
+            "k_bp": 4 * V + 4 * Sb, "k_update": 88 * V, "k_update_u": 28 * V, "k_update_p": 72 * V,
+            "k_dual_fused": 100 * V}
 
 
 def gather_bytes(N, nang, S):
@@ -360,7 +365,7 @@ def run_ours(args, rank, world, local):
            "roofline": roof,
            "kernels_ms": kms,
            "hbm_kernels": {k: {"achieved": alg[k] / (kms[k] / 1e3) / 1e9, "frac": alg[k] / (kms[k] / 1e3) / 1e9 / hbm}
-                           for k in ("k_dual", "k_update_u", "k_update_p")},
+                           for k in ("k_dual", "k_update_u", "k_update_p", "k_dual_fused") if k in kms},
            "solver_roofline": {"achieved": solver_gbs, "peak": hbm, "unit": "GB/s", "frac": solver_gbs / hbm,
                                "algorithmic_bytes_per_iteration": alg["iteration"]},
            "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
@@ -895,8 +900,9 @@ def main():
                     help="force the forward projector's launch shape (no autotuning); profiler captures")
     ap.add_argument("--bp-shape", type=int, default=None, help="force the back projector's launch shape")
     ap.add_argument("--dual-shape", type=int, default=None, help="force the dual kernel's launch shape")
-    ap.add_argument("--schedule", type=int, default=None, choices=[0, 1],
-                    help="force the iteration schedule (0: primal update after the projectors, 1: its p half beside them)")
+    ap.add_argument("--schedule", type=int, default=None, choices=[0, 1, 2],
+                    help="force the iteration schedule (0: primal update after the projectors, 1: its p half beside "
+                         "them, 2: its p half fused into the next dual kernel)")
     ap.add_argument("--quick", action="store_true",
                     help="only the device-timed region (no e2e, kernel timing or CPU baseline): profiler runs")
     args = ap.parse_args()

@@ -22,6 +22,8 @@
 
 namespace gt {
 cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st);
+bool dual_fused_ok(const IterParams &P, int tgv, int cpl);
+cudaError_t launch_dual_fused(const IterParams &P, int tgv, int cpl, cudaStream_t st);
 cudaError_t prepare_bp_tma();
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st);
 cudaError_t launch_bp(const IterParams &P, cudaStream_t st);
@@ -184,13 +186,15 @@ struct gt_problem {
   size_t ray_bytes = 0;
   void *gap_ws = nullptr;      // gap workspace (v~ planes + FP64 block partials), allocated on first gt_gap
   float *snap = nullptr;       // copy of (u, p, v, w, lambda) for gt_movement, allocated on first gt_snapshot
+  float *fused = nullptr;      // second (p, v, w) of schedule 2, allocated when that schedule is timed or set
   double pweight = 1.0;        // primal weight: sigma = w / sqrt(Lsqr), tau = 1 / (w sqrt(Lsqr)); 1 = reference
   double *mu64 = nullptr;
   gt::IterParams P{};
   bool autotune = true;
   cudaGraphExec_t g_one = nullptr, g_chunk = nullptr;
   int chunk = 16;
-  int schedule = 1;            // 1: p / pbar half of the primal update beside the projectors; 0: one update after them
+  int schedule = 1;            // 1: p / pbar half of the primal update beside the projectors; 0: one update after
+                               // them; 2: the p / pbar half fused into the next iteration's dual kernel
   bool schedule_set = false;   // chosen by gt_set_schedule (the autotuner leaves it)
   long long iters = 0;
   bool has_data = false;
@@ -224,11 +228,77 @@ int enqueue_iteration(gt_problem *p) {
   return GT_OK;
 }
 
+// Schedule 2: m iterations (m odd, >= 3) software-pipelined.  The p / pbar half of
+// iteration k's primal update runs inside iteration k + 1's dual kernel (the fused
+// form of k_dual_cl2), beside that iteration's projectors, and only the u / ubar
+// half follows the join.  The fused kernel reads p, v, w of one buffer set and
+// writes the next p, v, w to the other, so the sets alternate: iteration 0 runs the
+// plain dual kernel on the problem's own set, iterations 1 .. m - 1 alternate
+// between the sets (an even number of them, so the last writes the problem's own
+// set), and a last launch of the p half completes iteration m - 1 there, pbar
+// included.  Outside the pipeline the state is the same as after m plain
+// iterations, value for value (the fused kernel computes p and the dual update by
+// the same operations).
+int enqueue_pipelined(gt_problem *p, int m) {
+  gt::IterParams A = p->P;
+  A.p2 = p->fused;
+  A.v2 = p->fused + (size_t)p->K * p->d.vol;
+  A.w2 = A.v2 + (size_t)p->K * p->d.vol;
+  gt::IterParams B = A;
+  std::swap(B.p, B.p2);
+  std::swap(B.v, B.v2);
+  std::swap(B.w, B.w2);
+  for (int k = 0; k < m; ++k) {
+    const gt::IterParams &X = (k % 2 == 1) ? A : B;  // fused kernel input set
+    CK(cudaEventRecord(p->ev_fork, p->stream));
+    CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
+    CK(gt::launch_fwd(p->P, p->disc, p->side));
+    CK(gt::launch_bp(p->P, p->side));
+    if (k == 0) CK(gt::launch_dual(p->P, 1, p->cpl, p->stream));
+    else CK(gt::launch_dual_fused(X, 1, p->cpl, p->stream));
+    CK(cudaEventRecord(p->ev_join, p->side));
+    CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
+    gt::IterParams Q = p->P;  // the u half reads the v just written
+    if (k > 0) Q.v = X.v2;
+    CK(gt::launch_update(Q, 1, p->stream, 1));
+  }
+  CK(gt::launch_update(p->P, 1, p->stream, 2));
+  return GT_OK;
+}
+
+bool fused_available(const gt_problem *p) { return gt::dual_fused_ok(p->P, p->reg == GT_TGV, p->cpl); }
+
+// the second (p, v, w) set of schedule 2
+int ensure_fused(gt_problem *p) {
+  if (p->fused) return GT_OK;
+  const size_t n = (size_t)(2 * p->K + p->KW) * p->d.vol;
+  cudaError_t e = cudaMalloc(&p->fused, sizeof(float) * n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    p->fused = nullptr;
+    return cuda_err(e, "cudaMalloc (schedule 2 buffers)", __LINE__);
+  }
+  return GT_OK;
+}
+
+void free_fused(gt_problem *p) {
+  if (p->fused) cudaFree(p->fused);
+  p->fused = nullptr;
+}
+
+int chunk_len(const gt_problem *p) { return p->schedule == 2 ? 32 : p->chunk; }
+
 int capture(gt_problem *p, int n, cudaGraphExec_t *out) {
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
   int rc = GT_OK;
-  for (int k = 0; k < n && rc == GT_OK; ++k) rc = enqueue_iteration(p);
+  int k = 0;
+  if (p->schedule == 2 && n >= 3 && p->fused) {
+    const int m = n % 2 ? n : n - 1;
+    rc = enqueue_pipelined(p, m);
+    k = m;
+  }
+  for (; k < n && rc == GT_OK; ++k) rc = enqueue_iteration(p);
   cudaError_t e = cudaStreamEndCapture(p->stream, &g);
   if (rc != GT_OK) {
     if (g) cudaGraphDestroy(g);
@@ -336,6 +406,7 @@ int autotune(gt_problem *p) {
       int sched = 0;
       std::tie(p->P.fwd_cfg, p->P.bp_cfg, p->P.dual_cfg, sched) = it->second;
       if (!p->schedule_set) p->schedule = sched;
+      if (p->schedule == 2 && ensure_fused(p) != GT_OK) p->schedule = 0;  // no room for the second set
       return GT_OK;
     }
   }
@@ -400,14 +471,19 @@ int autotune(gt_problem *p) {
   // each, the faster kept; concurrency between the kernels decides, not their times
   // alone.  Problems below 8M voxel-channels keep schedule 1 (the two schedules are
   // within a few per cent there, e.g. 0.135 / 0.132 ms at 128^2 x 32 x 2).
+  // Schedule 2 (the p half fused into the next dual kernel) is timed where the
+  // fused kernel applies and its second (p, v, w) set can be allocated; the set is
+  // freed again if another schedule wins.  Its graphs are timed over 16 iterations
+  // (15 pipelined), the others' likewise.
   if (tgv && !p->schedule_set && p->d.vol < (8u << 20)) p->schedule = 1;
   if (tgv && !p->schedule_set && p->d.vol >= (8u << 20)) {
-    float ms_s[2] = {1e30f, 1e30f};
+    const int nsched = (fused_available(p) && ensure_fused(p) == GT_OK) ? 3 : 2;
+    float ms_s[3] = {1e30f, 1e30f, 1e30f};
     for (int round = 0; round < 2 && rc == GT_OK; ++round) {
-      for (int sched = 0; sched < 2 && rc == GT_OK; ++sched) {
+      for (int sched = 0; sched < nsched && rc == GT_OK; ++sched) {
         p->schedule = sched;
         cudaGraphExec_t g = nullptr;
-        rc = capture(p, 8, &g);
+        rc = capture(p, 16, &g);
         if (rc) break;
         cudaError_t e = cudaGraphLaunch(g, p->stream);
         if (e == cudaSuccess) e = cudaEventRecord(e0, p->stream);
@@ -418,12 +494,17 @@ int autotune(gt_problem *p) {
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
         cudaGraphExecDestroy(g);
         if (e != cudaSuccess) { rc = cuda_err(e, "autotune (schedule)", __LINE__); break; }
-        ms_s[sched] = std::min(ms_s[sched], ms / 16);
+        ms_s[sched] = std::min(ms_s[sched], ms / 32);
       }
     }
-    p->schedule = ms_s[1] < ms_s[0] ? 1 : 0;
+    int bs = 0;
+    for (int sched = 1; sched < nsched; ++sched)
+      if (ms_s[sched] < ms_s[bs]) bs = sched;
+    p->schedule = bs;
+    if (bs != 2) free_fused(p);
     if (log && rc == GT_OK)
-      fprintf(stderr, "graptor autotune schedule 0: %.4f ms, 1: %.4f ms per iteration\n", ms_s[0], ms_s[1]);
+      fprintf(stderr, "graptor autotune schedule 0: %.4f ms, 1: %.4f ms, 2: %.4f ms per iteration\n", ms_s[0],
+              ms_s[1], ms_s[2]);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -453,9 +534,17 @@ int gt_launches_per_iteration(const gt_problem *p) {
 
 int gt_set_schedule(gt_problem *p, int schedule) {
   if (!p) return set_err(GT_ERR_ARG, "null argument");
-  if (schedule != 0 && schedule != 1) return set_err(GT_ERR_ARG, "schedule must be 0 or 1 (got %d)", schedule);
+  if (schedule < 0 || schedule > 2) return set_err(GT_ERR_ARG, "schedule must be 0, 1 or 2 (got %d)", schedule);
+  if (schedule == 2 && !fused_available(p))
+    return set_err(GT_ERR_ARG, "schedule 2 needs 3-D TGV, Frobenius or uncorrelated coupling, C <= 4 and Nz even");
   CK(cudaSetDevice(p->device));
   CK(cudaStreamSynchronize(p->stream));
+  if (schedule == 2) {
+    const int rc = ensure_fused(p);
+    if (rc) return rc;
+  } else {
+    free_fused(p);
+  }
   p->schedule = schedule;
   p->schedule_set = true;
   if (p->g_one) { cudaGraphExecDestroy(p->g_one); p->g_one = nullptr; }
@@ -690,6 +779,7 @@ void gt_problem_destroy(gt_problem *p) {
   if (p->tiles) cudaFree(p->tiles);
   if (p->gap_ws) cudaFree(p->gap_ws);
   if (p->snap) cudaFree(p->snap);
+  if (p->fused) cudaFree(p->fused);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
   if (p->side) cudaStreamDestroy(p->side);
@@ -768,10 +858,16 @@ int gt_run(gt_problem *p, int iters) {
   if (iters == 0) return GT_OK;
   CK(cudaSetDevice(p->device));
   int rc;
-  if (iters >= p->chunk && !p->g_chunk && (rc = capture(p, p->chunk, &p->g_chunk)) != GT_OK) return rc;
+  const int chunk = chunk_len(p);
+  if (iters >= chunk && !p->g_chunk && (rc = capture(p, chunk, &p->g_chunk)) != GT_OK) return rc;
   if (!p->g_one && (rc = capture(p, 1, &p->g_one)) != GT_OK) return rc;
   int left = iters;
-  while (left >= p->chunk) { CK(cudaGraphLaunch(p->g_chunk, p->stream)); left -= p->chunk; }
+  while (left >= chunk) { CK(cudaGraphLaunch(p->g_chunk, p->stream)); left -= chunk; }
+  if (p->schedule == 2 && p->fused && left >= 3) {  // the rest pipelined too, launched directly
+    const int m = left % 2 ? left : left - 1;
+    if ((rc = enqueue_pipelined(p, m)) != GT_OK) return rc;
+    left -= m;
+  }
   while (left > 0) { CK(cudaGraphLaunch(p->g_one, p->stream)); --left; }
   p->iters += iters;
   return GT_OK;
@@ -1111,6 +1207,30 @@ int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n) {
       acc[k] += ms;
     }
     p->iters += 1;
+  }
+  // n >= 7: the fused dual kernel of schedule 2 into ms_out[6] (0 where it does not
+  // apply or its second buffer set does not exist).  It reads the state and writes
+  // only that second set, so the state does not change.
+  if (n >= 7) {
+    ms_out[6] = 0.f;
+    if (rc == GT_OK && p->fused && fused_available(p)) {
+      gt::IterParams Q = p->P;
+      Q.p2 = p->fused;
+      Q.v2 = p->fused + (size_t)p->K * p->d.vol;
+      Q.w2 = Q.v2 + (size_t)p->K * p->d.vol;
+      float tot = 0.f;
+      for (int r = 0; r < reps && rc == GT_OK; ++r) {
+        cudaError_t e = cudaEventRecord(ev[0], p->stream);
+        if (e == cudaSuccess) e = gt::launch_dual_fused(Q, 1, p->cpl, p->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], p->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        if (e != cudaSuccess) { rc = cuda_err(e, "kernel timing (fused dual)", __LINE__); break; }
+        tot += ms;
+      }
+      ms_out[6] = tot / reps;
+    }
   }
   for (auto &e : ev) cudaEventDestroy(e);
   if (rc) return rc;

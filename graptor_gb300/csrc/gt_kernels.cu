@@ -220,6 +220,25 @@ __device__ __forceinline__ float wnorm2(const float *w) {
   }
 }
 
+// One component of update_p (3-D :734-757) at one voxel-slice: the divergence of
+// the symmetric tensor w by forward differences (wa, wb, wc the row's entries at the
+// voxel, wan, wbn, wcn at its x / y / z successor; fx, fy, fz: first pixel / row /
+// slice, hx, hy, hz: a successor exists), then p + tau (v + div w).  k_update and the
+// fused dual kernel both compute p through this function, by the same operations.
+__device__ __forceinline__ float p_step3(float po, float vk, float wa, float wan, float wb, float wbn, float wc,
+                                         float wcn, bool fx, bool hx, bool fy, bool hy, bool fz, bool hz, float tau,
+                                         float stepsize) {
+  float A = -wa, B = -wb, Cz = -wc;
+  if (fx) A = 0.f;
+  if (hx) A += wan;
+  if (fy) B = 0.f;
+  if (hy) B += wbn;
+  if (fz) Cz = 0.f;
+  if (hz) Cz += wcn;
+  Cz /= stepsize;
+  return po + tau * (vk + A + B + Cz);
+}
+
 // projections of the dual variables onto the norm balls (NormV / NormW of the
 // coupling): vv, ww of the nC channels of one voxel, in place.
 template <int DIM, bool TGV, int CPL, int CMAX>
@@ -667,12 +686,64 @@ __global__ void __launch_bounds__(256) k_dual_cl(const IterParams P) {
 __device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
 __device__ __forceinline__ void st2(float *p, float a, float b) { *reinterpret_cast<float2 *>(p) = make_float2(a, b); }
 
+// pbar (and p) of the slice pair (z0, z0 + 1) at offset j, pixel (xj, yj), from the
+// p, v, w of the iterate in P.p, P.v, P.w: update_p (3-D :734-757) and its
+// extrapolation (:1217-1221) through p_step3.  wj, vj: w and v at j; wx: rows
+// (w0 w3 w4) at the x successor (read where xj < N - 1); wy: rows (w3 w1 w5) at
+// the y successor (yj < N - 1); wz: rows (w4 w5 w2) at slice z0 + 2 (z0 + 1 < Nz - 1).
+__device__ __forceinline__ void pair_pstep(const IterParams &P, size_t j, int xj, int yj, int z0,
+                                           const float2 (&wj)[6], const float2 (&vj)[3], const float2 (&wx)[3],
+                                           const float2 (&wy)[3], const float (&wz)[3], float2 (&pn)[3],
+                                           float2 (&pbr)[3]) {
+  const Dims d = P.d;
+  const size_t vol = d.vol;
+  const int rx[3] = {0, 3, 4}, ry[3] = {3, 1, 5}, rz[3] = {4, 5, 2};
+  const bool fx = xj == 0, hx = xj < d.N - 1, fy = yj == 0, hy = yj < d.N - 1;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float2 po = ld2(P.p + k * vol + j);
+    const float r0 = p_step3(po.x, vj[k].x, wj[rx[k]].x, wx[k].x, wj[ry[k]].x, wy[k].x, wj[rz[k]].x, wj[rz[k]].y,
+                             fx, hx, fy, hy, z0 == 0, true, P.tau, P.stepsize);
+    const float r1 = p_step3(po.y, vj[k].y, wj[rx[k]].y, wx[k].y, wj[ry[k]].y, wy[k].y, wj[rz[k]].y, wz[k], fx, hx,
+                             fy, hy, false, z0 + 1 < d.Nz - 1, P.tau, P.stepsize);
+    pn[k] = make_float2(r0, r1);
+    pbr[k] = make_float2(2.0f * r0 - po.x, 2.0f * r1 - po.y);
+  }
+}
+
+// pair_pstep for the one slice z (z >= 1) at offset j: wz holds rows (w4 w5 w2) at z + 1.
+__device__ __forceinline__ void slice_pstep(const IterParams &P, size_t j, int xj, int yj, int z,
+                                            const float (&wj)[6], const float (&vj)[3], const float (&wx)[3],
+                                            const float (&wy)[3], const float (&wz)[3], float (&pbr)[3]) {
+  const Dims d = P.d;
+  const size_t vol = d.vol;
+  const int rx[3] = {0, 3, 4}, ry[3] = {3, 1, 5}, rz[3] = {4, 5, 2};
+  const bool fx = xj == 0, hx = xj < d.N - 1, fy = yj == 0, hy = yj < d.N - 1;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float po = P.p[k * vol + j];
+    const float r = p_step3(po, vj[k], wj[rx[k]], wx[k], wj[ry[k]], wy[k], wj[rz[k]], wz[k], fx, hx, fy, hy, z == 0,
+                            z < d.Nz - 1, P.tau, P.stepsize);
+    pbr[k] = 2.0f * r - po;
+  }
+}
+
 // k_dual_cl2: k_dual_cl for two consecutive slices z0, z0 + 1 of one channel per
 // thread (3-D, Nz even): the fields of both slices move as one float2, the slice
 // neighbours outside the pair as one float each.  Per slice the arithmetic and the
 // shuffle order are k_dual_cl's, so the iterates are bit-identical to k_dual's.
-template <bool TGV, int CPL, int CP>
+//
+// FUSED (3-D TGV): the p / pbar half of the previous iteration's primal update is
+// computed here instead of in k_update.  pbar at the thread's pair and at its
+// x, y and z predecessors (the symmetric gradient's backward differences) comes
+// from p, v, w of P.p, P.v, P.w through pair_pstep / slice_pstep; the new p of the
+// pair goes to P.p2 and the dual update of v, w to P.v2, P.w2 (other buffers: the
+// neighbours' p, v, w must stay unchanged while other blocks read them).  The pbar
+// buffer is neither read nor written, and every value is computed by the same
+// operations as in k_update and the unfused kernel (bit-identical iterates).
+template <bool TGV, int CPL, int CP, bool FUSED = false>
 __global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
+  static_assert(!FUSED || TGV, "the fused form needs the TGV fields");
   constexpr int K = 3, KW = 6;
   const Dims d = P.d;
   const int nz2 = d.Nz >> 1;
@@ -701,6 +772,9 @@ __global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
   for (int k = 0; k < K; ++k) { p0[k] = px[k] = py[k] = vo[k] = u0; pzm[k] = 0.f; }
 #pragma unroll
   for (int k = 0; k < KW; ++k) wo[k] = u0;
+  float2 pn[K];  // FUSED: p of the pair
+#pragma unroll
+  for (int k = 0; k < K; ++k) pn[k] = u0;
   if (own) {
     u0 = ld2(ub + i);
     if (hx) ux = ld2(ub + i + S);
@@ -709,7 +783,7 @@ __global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       vo[k] = ld2(P.v + k * vol + i);
-      if (TGV) {
+      if (TGV && !FUSED) {
         p0[k] = ld2(pb + k * vol + i);
         if (lx) px[k] = ld2(pb + k * vol + i - S);
         if (ly) py[k] = ld2(pb + k * vol + i - rowS);
@@ -719,6 +793,66 @@ __global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
     if (TGV) {
 #pragma unroll
       for (int k = 0; k < KW; ++k) wo[k] = ld2(P.w + k * vol + i);
+    }
+    if constexpr (FUSED) {
+      const float *__restrict__ w = P.w;
+      const int rx[3] = {0, 3, 4}, ry[3] = {3, 1, 5}, rz[3] = {4, 5, 2};
+      const float2 zero = make_float2(0.f, 0.f);
+      {  // the pair itself
+        float2 wx[3], wy[3];
+        float wz[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          wx[k] = hx ? ld2(w + rx[k] * vol + i + S) : zero;
+          wy[k] = hy ? ld2(w + ry[k] * vol + i + rowS) : zero;
+          wz[k] = hz[1] ? w[rz[k] * vol + i + 2] : 0.f;
+        }
+        pair_pstep(P, i, x, y, z0, wo, vo, wx, wy, wz, pn, p0);
+      }
+      if (lx) {  // x predecessor: its x successor is this pixel
+        const size_t j = i - S;
+        float2 wj[6], vj[3], wx[3], wy[3], unused[3];
+        float wz[3];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) wj[k] = ld2(w + k * vol + j);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          vj[k] = ld2(P.v + k * vol + j);
+          wx[k] = wo[rx[k]];
+          wy[k] = hy ? ld2(w + ry[k] * vol + j + rowS) : zero;
+          wz[k] = hz[1] ? w[rz[k] * vol + j + 2] : 0.f;
+        }
+        pair_pstep(P, j, x - 1, y, z0, wj, vj, wx, wy, wz, unused, px);
+      }
+      if (ly) {  // y predecessor: its y successor is this pixel
+        const size_t j = i - rowS;
+        float2 wj[6], vj[3], wx[3], wy[3], unused[3];
+        float wz[3];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) wj[k] = ld2(w + k * vol + j);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          vj[k] = ld2(P.v + k * vol + j);
+          wx[k] = hx ? ld2(w + rx[k] * vol + j + S) : zero;
+          wy[k] = wo[ry[k]];
+          wz[k] = hz[1] ? w[rz[k] * vol + j + 2] : 0.f;
+        }
+        pair_pstep(P, j, x, y - 1, z0, wj, vj, wx, wy, wz, unused, py);
+      }
+      if (lz[0]) {  // slice z0 - 1: its z successor is the pair's first slice
+        const size_t j = i - 1;
+        float wj[6], vj[3], wx[3], wy[3], wz[3];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) wj[k] = w[k * vol + j];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          vj[k] = P.v[k * vol + j];
+          wx[k] = hx ? w[rx[k] * vol + j + S] : 0.f;
+          wy[k] = hy ? w[ry[k] * vol + j + rowS] : 0.f;
+          wz[k] = wo[rz[k]].x;
+        }
+        slice_pstep(P, j, x, y, z0 - 1, wj, vj, wx, wy, wz, pzm);
+      }
     }
   }
 
@@ -812,11 +946,16 @@ __global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
   }
 
   if (own) {
+    float *vout = FUSED ? P.v2 : P.v, *wout = FUSED ? P.w2 : P.w;
 #pragma unroll
-    for (int k = 0; k < K; ++k) st2(P.v + k * vol + i, vv[0][k], vv[1][k]);
+    for (int k = 0; k < K; ++k) st2(vout + k * vol + i, vv[0][k], vv[1][k]);
     if (TGV) {
 #pragma unroll
-      for (int k = 0; k < KW; ++k) st2(P.w + k * vol + i, ww[0][k], ww[1][k]);
+      for (int k = 0; k < KW; ++k) st2(wout + k * vol + i, ww[0][k], ww[1][k]);
+    }
+    if (FUSED) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) st2(P.p2 + k * vol + i, pn[k].x, pn[k].y);
     }
   }
 }
@@ -1661,11 +1800,8 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
         if (y < d.N - 1) B += wbn[e];
         float r;
         if (DIM == 3) {
-          float Cz = -wc[e];
-          if (z[e] == 0) Cz = 0.f;
-          if (z[e] < d.Nz - 1) Cz += (e < UW - 1 ? wc[e + 1] : wcnext);
-          Cz /= P.stepsize;
-          r = po[e] + P.tau * (vk[e] + A + B + Cz);
+          r = p_step3(po[e], vk[e], wa[e], wan[e], wb[e], wbn[e], wc[e], e < UW - 1 ? wc[e + 1] : wcnext, x == 0,
+                      x < d.N - 1, y == 0, y < d.N - 1, z[e] == 0, z[e] < d.Nz - 1, P.tau, P.stepsize);
         } else {
           r = po[e] + P.tau * (vk[e] + A + B);
         }
@@ -2636,6 +2772,27 @@ static cudaError_t launch_dual_t(const IterParams &P, int cpl, cudaStream_t st) 
 cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st) {
   if (P.d.dim == 3) return tgv ? launch_dual_t<3, true>(P, cpl, st) : launch_dual_t<3, false>(P, cpl, st);
   return tgv ? launch_dual_t<2, true>(P, cpl, st) : launch_dual_t<2, false>(P, cpl, st);
+}
+
+// the fused dual kernel (k_dual_cl2<..., FUSED>): 3-D TGV, Frobenius or
+// uncorrelated coupling, C <= 4, Nz even
+bool dual_fused_ok(const IterParams &P, int tgv, int cpl) { return tgv && dual_cl2_ok(P, cpl); }
+
+cudaError_t launch_dual_fused(const IterParams &P, int tgv, int cpl, cudaStream_t st) {
+  if (!dual_fused_ok(P, tgv, cpl) || !P.p2 || !P.v2 || !P.w2) return cudaErrorInvalidValue;
+  const int C = P.d.C;
+  const int cp = C <= 1 ? 1 : (C <= 2 ? 2 : 4);
+  const unsigned g = blocks_for((long long)P.d.N * P.d.N * (P.d.Nz / 2) * cp, 128);
+  if (cpl == UNCORR) {
+    if (cp == 1) k_dual_cl2<true, UNCORR, 1, true><<<g, 128, 0, st>>>(P);
+    else if (cp == 2) k_dual_cl2<true, UNCORR, 2, true><<<g, 128, 0, st>>>(P);
+    else k_dual_cl2<true, UNCORR, 4, true><<<g, 128, 0, st>>>(P);
+  } else {
+    if (cp == 1) k_dual_cl2<true, FROB, 1, true><<<g, 128, 0, st>>>(P);
+    else if (cp == 2) k_dual_cl2<true, FROB, 2, true><<<g, 128, 0, st>>>(P);
+    else k_dual_cl2<true, FROB, 4, true><<<g, 128, 0, st>>>(P);
+  }
+  return cudaGetLastError();
 }
 
 // Forward projection of R adjacent bins of one angle at once.  For every row the

@@ -170,7 +170,8 @@ class Problem:
 
     def set_schedule(self, schedule: int):
         """1: the p / pbar half of the primal update beside the projectors (default);
-        0: the whole primal update after them (see gt_set_schedule)."""
+        0: the whole primal update after them; 2: the p / pbar half fused into the
+        next iteration's dual kernel (3-D TGV; see gt_set_schedule)."""
         L.check(L.lib().gt_set_schedule(self._h, int(schedule)))
         return self
 
@@ -259,11 +260,16 @@ class Problem:
 
     def time_kernels(self, reps: int = 5) -> dict:
         """Mean CUDA-event duration (ms) of each kernel of one iteration; the
-        primal update as a whole (k_update) and as its u / ubar and p / pbar halves."""
-        out = (ctypes.c_float * 6)()
-        L.check(L.lib().gt_time_kernels(self._h, int(reps), out, 6))
-        return {"k_dual": out[0], "k_fwd": out[1], "k_bp": out[2], "k_update": out[3], "k_update_u": out[4],
-                "k_update_p": out[5]}
+        primal update as a whole (k_update) and as its u / ubar and p / pbar halves;
+        k_dual_fused: the fused dual kernel of schedule 2 where that schedule is set
+        (absent otherwise)."""
+        out = (ctypes.c_float * 7)()
+        L.check(L.lib().gt_time_kernels(self._h, int(reps), out, 7))
+        r = {"k_dual": out[0], "k_fwd": out[1], "k_bp": out[2], "k_update": out[3], "k_update_u": out[4],
+             "k_update_p": out[5]}
+        if out[6] > 0:
+            r["k_dual_fused"] = out[6]
+        return r
 
     @property
     def launches_per_iteration(self) -> int:

@@ -122,10 +122,16 @@ GT_API int gt_get_dual_shape(gt_problem *p);
  * its extrapolation, radon_tgv_primal_dual_3d.py:734-757, :1217-1221) runs right
  * after the dual update, beside the projector chain, and only the u / ubar half
  * (update_u, :706-729) waits for the back projection; 0: the whole primal update
- * runs after the back projection.  The reference enqueues update_u then update_p
- * after radon_ad (:1194-1221); both schedules give bit-identical iterates.  The
- * autotuner (gt_set_data) times both as graph-captured iterations and keeps the
- * faster, unless gt_set_schedule chose one; gt_get_schedule returns the current. */
+ * runs after the back projection; 2 (3-D TGV, Frobenius or uncorrelated coupling,
+ * C <= 4, Nz even): the p / pbar half of each iteration is computed inside the
+ * next iteration's dual kernel (pbar at a voxel and its three predecessors from p,
+ * v, w), which writes p, v, w to a second buffer set (12 floats per voxel-channel,
+ * allocated by this call or the autotuner); the sets alternate within a run of
+ * gt_run and every gt_run ends on the problem's own set with the state of plain
+ * iterations.  The reference enqueues update_u then update_p after radon_ad
+ * (:1194-1221); all schedules give bit-identical iterates.  The autotuner
+ * (gt_set_data) times them as graph-captured iterations and keeps the fastest,
+ * unless gt_set_schedule chose one; gt_get_schedule returns the current. */
 GT_API int gt_set_schedule(gt_problem *p, int schedule);
 GT_API int gt_get_schedule(gt_problem *p);
 
@@ -183,7 +189,9 @@ GT_API int gt_radon_ad(const float *sino_dev, float *img_dev, const double *angl
  * mean duration of k_dual, k_fwd, k_bp and k_update (n >= 4); with n >= 6 the
  * update runs as its two halves, ms_out[4] and ms_out[5] receive the u / ubar and
  * the p / pbar half and ms_out[3] their sum.  The iterations are real: the state
- * advances by reps iterations. */
+ * advances by reps iterations.  With n >= 7, ms_out[6] receives the fused dual
+ * kernel of schedule 2 (timed afterwards on the state, into the second buffer set
+ * only; 0 when schedule 2 is not set or does not apply). */
 GT_API int gt_time_kernels(gt_problem *p, int reps, float *ms_out, int n);
 
 /* Allocation-free operator-norm estimate.  No counterpart in the reference (which
