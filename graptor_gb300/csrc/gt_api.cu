@@ -24,6 +24,7 @@ namespace gt {
 cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st);
 bool dual_fused_ok(const IterParams &P, int tgv, int cpl);
 cudaError_t launch_dual_fused(const IterParams &P, int tgv, int cpl, cudaStream_t st);
+cudaError_t prepare_dual_fused(const IterParams &P, int cpl);
 cudaError_t prepare_bp_tma();
 cudaError_t launch_fwd(const IterParams &P, int disc, cudaStream_t st);
 cudaError_t launch_bp(const IterParams &P, cudaStream_t st);
@@ -272,7 +273,9 @@ bool fused_available(const gt_problem *p) { return gt::dual_fused_ok(p->P, p->re
 int ensure_fused(gt_problem *p) {
   if (p->fused) return GT_OK;
   const size_t n = (size_t)(2 * p->K + p->KW) * p->d.vol;
-  cudaError_t e = cudaMalloc(&p->fused, sizeof(float) * n);
+  cudaError_t e = gt::prepare_dual_fused(p->P, p->cpl);
+  if (e != cudaSuccess) return cuda_err(e, "cudaFuncSetAttribute (fused dual kernel)", __LINE__);
+  e = cudaMalloc(&p->fused, sizeof(float) * n);
   if (e != cudaSuccess) {
     cudaGetLastError();
     p->fused = nullptr;
@@ -471,13 +474,13 @@ int autotune(gt_problem *p) {
   // each, the faster kept; concurrency between the kernels decides, not their times
   // alone.  Problems below 8M voxel-channels keep schedule 1 (the two schedules are
   // within a few per cent there, e.g. 0.135 / 0.132 ms at 128^2 x 32 x 2).
-  // Schedule 2 (the p half fused into the next dual kernel) is timed where the
-  // fused kernel applies and its second (p, v, w) set can be allocated; the set is
-  // freed again if another schedule wins.  Its graphs are timed over 16 iterations
-  // (15 pipelined), the others' likewise.
+  // Schedule 2 (the p half fused into the next dual kernel) is not timed: its
+  // fused kernel is slower than the dual kernel and the p half together on every
+  // measured workload (256^2 x 60 x 4: 1.07 ms against 0.25 + 0.16 ms), so it
+  // stays a choice of gt_set_schedule.  The graphs are timed over 16 iterations.
   if (tgv && !p->schedule_set && p->d.vol < (8u << 20)) p->schedule = 1;
   if (tgv && !p->schedule_set && p->d.vol >= (8u << 20)) {
-    const int nsched = (fused_available(p) && ensure_fused(p) == GT_OK) ? 3 : 2;
+    const int nsched = 2;
     float ms_s[3] = {1e30f, 1e30f, 1e30f};
     for (int round = 0; round < 2 && rc == GT_OK; ++round) {
       for (int sched = 0; sched < nsched && rc == GT_OK; ++sched) {

@@ -686,178 +686,47 @@ __global__ void __launch_bounds__(256) k_dual_cl(const IterParams P) {
 __device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
 __device__ __forceinline__ void st2(float *p, float a, float b) { *reinterpret_cast<float2 *>(p) = make_float2(a, b); }
 
-// pbar (and p) of the slice pair (z0, z0 + 1) at offset j, pixel (xj, yj), from the
-// p, v, w of the iterate in P.p, P.v, P.w: update_p (3-D :734-757) and its
-// extrapolation (:1217-1221) through p_step3.  wj, vj: w and v at j; wx: rows
-// (w0 w3 w4) at the x successor (read where xj < N - 1); wy: rows (w3 w1 w5) at
-// the y successor (yj < N - 1); wz: rows (w4 w5 w2) at slice z0 + 2 (z0 + 1 < Nz - 1).
-__device__ __forceinline__ void pair_pstep(const IterParams &P, size_t j, int xj, int yj, int z0,
+// pbar and p of the slice pair (z0, z0 + 1) at offset j, pixel (xj, yj): update_p
+// (3-D :734-757) and its extrapolation (:1217-1221) through p_step3.  po, vj, wj:
+// p, v and w at j; wx: rows (w0 w3 w4) of w at the x successor (read where
+// xj < N - 1); wy: rows (w3 w1 w5) at the y successor (yj < N - 1); wz: rows
+// (w4 w5 w2) at slice z0 + 2 (z0 + 1 < Nz - 1).
+__device__ __forceinline__ void pair_pstep(const IterParams &P, int xj, int yj, int z0, const float2 (&po)[3],
                                            const float2 (&wj)[6], const float2 (&vj)[3], const float2 (&wx)[3],
                                            const float2 (&wy)[3], const float (&wz)[3], float2 (&pn)[3],
                                            float2 (&pbr)[3]) {
   const Dims d = P.d;
-  const size_t vol = d.vol;
   const int rx[3] = {0, 3, 4}, ry[3] = {3, 1, 5}, rz[3] = {4, 5, 2};
   const bool fx = xj == 0, hx = xj < d.N - 1, fy = yj == 0, hy = yj < d.N - 1;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float2 po = ld2(P.p + k * vol + j);
-    const float r0 = p_step3(po.x, vj[k].x, wj[rx[k]].x, wx[k].x, wj[ry[k]].x, wy[k].x, wj[rz[k]].x, wj[rz[k]].y,
-                             fx, hx, fy, hy, z0 == 0, true, P.tau, P.stepsize);
-    const float r1 = p_step3(po.y, vj[k].y, wj[rx[k]].y, wx[k].y, wj[ry[k]].y, wy[k].y, wj[rz[k]].y, wz[k], fx, hx,
-                             fy, hy, false, z0 + 1 < d.Nz - 1, P.tau, P.stepsize);
+    const float r0 = p_step3(po[k].x, vj[k].x, wj[rx[k]].x, wx[k].x, wj[ry[k]].x, wy[k].x, wj[rz[k]].x,
+                             wj[rz[k]].y, fx, hx, fy, hy, z0 == 0, true, P.tau, P.stepsize);
+    const float r1 = p_step3(po[k].y, vj[k].y, wj[rx[k]].y, wx[k].y, wj[ry[k]].y, wy[k].y, wj[rz[k]].y, wz[k], fx,
+                             hx, fy, hy, false, z0 + 1 < d.Nz - 1, P.tau, P.stepsize);
     pn[k] = make_float2(r0, r1);
-    pbr[k] = make_float2(2.0f * r0 - po.x, 2.0f * r1 - po.y);
+    pbr[k] = make_float2(2.0f * r0 - po[k].x, 2.0f * r1 - po[k].y);
   }
 }
 
-// pair_pstep for the one slice z (z >= 1) at offset j: wz holds rows (w4 w5 w2) at z + 1.
-__device__ __forceinline__ void slice_pstep(const IterParams &P, size_t j, int xj, int yj, int z,
-                                            const float (&wj)[6], const float (&vj)[3], const float (&wx)[3],
-                                            const float (&wy)[3], const float (&wz)[3], float (&pbr)[3]) {
-  const Dims d = P.d;
-  const size_t vol = d.vol;
-  const int rx[3] = {0, 3, 4}, ry[3] = {3, 1, 5}, rz[3] = {4, 5, 2};
-  const bool fx = xj == 0, hx = xj < d.N - 1, fy = yj == 0, hy = yj < d.N - 1;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float po = P.p[k * vol + j];
-    const float r = p_step3(po, vj[k], wj[rx[k]], wx[k], wj[ry[k]], wy[k], wj[rz[k]], wz[k], fx, hx, fy, hy, z == 0,
-                            z < d.Nz - 1, P.tau, P.stepsize);
-    pbr[k] = 2.0f * r - po;
-  }
-}
-
-// k_dual_cl2: k_dual_cl for two consecutive slices z0, z0 + 1 of one channel per
-// thread (3-D, Nz even): the fields of both slices move as one float2, the slice
-// neighbours outside the pair as one float each.  Per slice the arithmetic and the
-// shuffle order are k_dual_cl's, so the iterates are bit-identical to k_dual's.
-//
-// FUSED (3-D TGV): the p / pbar half of the previous iteration's primal update is
-// computed here instead of in k_update.  pbar at the thread's pair and at its
-// x, y and z predecessors (the symmetric gradient's backward differences) comes
-// from p, v, w of P.p, P.v, P.w through pair_pstep / slice_pstep; the new p of the
-// pair goes to P.p2 and the dual update of v, w to P.v2, P.w2 (other buffers: the
-// neighbours' p, v, w must stay unchanged while other blocks read them).  The pbar
-// buffer is neither read nor written, and every value is computed by the same
-// operations as in k_update and the unfused kernel (bit-identical iterates).
-template <bool TGV, int CPL, int CP, bool FUSED = false>
-__global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
-  static_assert(!FUSED || TGV, "the fused form needs the TGV fields");
+// The dual update of one channel's slice pair (z0, z0 + 1) of one voxel column,
+// k_dual_cl's arithmetic and shuffle order per slice: v + sigma (grad ubar - pbar)
+// and w + sigma E(pbar) (update_v :546-571, update_w :573-600), projected onto the
+// coupling's balls (NormV / NormW).  The CP lanes of a voxel (from lane0) hold its
+// channels; every lane of the warp must call this (shuffles).  Inputs: ubar at
+// the pair (u0), its x / y successors (ux, uy) and slice z0 + 2 (uz1); pbar at the
+// pair (p0), its x / y predecessors (px, py) and slice z0 - 1 (pzm); v, w at the pair.
+// STEP1: the slice step size is 1, so the divisions by it (x / 1 = x exactly in IEEE
+// arithmetic) are left out; the results are the same bits.
+template <bool TGV, int CPL, int CP, bool STEP1 = false>
+__device__ __forceinline__ void dual_pair_math(const IterParams &P, unsigned lane0, float2 u0, float2 ux, float2 uy,
+                                               float uz1, const float2 (&p0)[3], const float2 (&px)[3],
+                                               const float2 (&py)[3], const float (&pzm)[3], const float2 (&vo)[3],
+                                               const float2 (&wo)[6], bool hx, bool hy, bool lx, bool ly, int z0,
+                                               float (&vv)[2][3], float (&ww)[2][6]) {
   constexpr int K = 3, KW = 6;
-  const Dims d = P.d;
-  const int nz2 = d.Nz >> 1;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long vt = t / CP;  // (pixel, slice pair)
-  const int c = (int)(t - vt * CP);
-  const bool valid = vt < (long long)d.N * d.N * nz2;
-  const bool own = valid && c < d.C;
-  const int pix = valid ? (int)(vt / nz2) : 0;
-  const int z0 = valid ? 2 * (int)(vt - (long long)pix * nz2) : 0;
-  const int y = pix / d.N, x = pix - y * d.N;
-  const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
-  const bool hx = x < d.N - 1, hy = y < d.N - 1;
-  const bool lx = x > 0, ly = y > 0;
-  const bool hz[2] = {true, z0 + 1 < d.Nz - 1}, lz[2] = {z0 > 0, true};
-  const float *__restrict__ ub = P.ubar;
-  const float *__restrict__ pb = P.pbar;
-  const size_t i = (size_t)pix * S + (size_t)c * d.Nz + z0;
-  const unsigned lane0 = (threadIdx.x & 31) & ~(unsigned)(CP - 1);
-
-  float2 u0 = make_float2(0.f, 0.f), ux = u0, uy = u0;
-  float uz1 = 0.f;  // ubar at z0 + 2
-  float2 p0[K], px[K], py[K], vo[K], wo[KW];
-  float pzm[K];  // pbar at z0 - 1
-#pragma unroll
-  for (int k = 0; k < K; ++k) { p0[k] = px[k] = py[k] = vo[k] = u0; pzm[k] = 0.f; }
-#pragma unroll
-  for (int k = 0; k < KW; ++k) wo[k] = u0;
-  float2 pn[K];  // FUSED: p of the pair
-#pragma unroll
-  for (int k = 0; k < K; ++k) pn[k] = u0;
-  if (own) {
-    u0 = ld2(ub + i);
-    if (hx) ux = ld2(ub + i + S);
-    if (hy) uy = ld2(ub + i + rowS);
-    if (hz[1]) uz1 = ub[i + 2];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      vo[k] = ld2(P.v + k * vol + i);
-      if (TGV && !FUSED) {
-        p0[k] = ld2(pb + k * vol + i);
-        if (lx) px[k] = ld2(pb + k * vol + i - S);
-        if (ly) py[k] = ld2(pb + k * vol + i - rowS);
-        if (lz[0]) pzm[k] = pb[k * vol + i - 1];
-      }
-    }
-    if (TGV) {
-#pragma unroll
-      for (int k = 0; k < KW; ++k) wo[k] = ld2(P.w + k * vol + i);
-    }
-    if constexpr (FUSED) {
-      const float *__restrict__ w = P.w;
-      const int rx[3] = {0, 3, 4}, ry[3] = {3, 1, 5}, rz[3] = {4, 5, 2};
-      const float2 zero = make_float2(0.f, 0.f);
-      {  // the pair itself
-        float2 wx[3], wy[3];
-        float wz[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          wx[k] = hx ? ld2(w + rx[k] * vol + i + S) : zero;
-          wy[k] = hy ? ld2(w + ry[k] * vol + i + rowS) : zero;
-          wz[k] = hz[1] ? w[rz[k] * vol + i + 2] : 0.f;
-        }
-        pair_pstep(P, i, x, y, z0, wo, vo, wx, wy, wz, pn, p0);
-      }
-      if (lx) {  // x predecessor: its x successor is this pixel
-        const size_t j = i - S;
-        float2 wj[6], vj[3], wx[3], wy[3], unused[3];
-        float wz[3];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) wj[k] = ld2(w + k * vol + j);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          vj[k] = ld2(P.v + k * vol + j);
-          wx[k] = wo[rx[k]];
-          wy[k] = hy ? ld2(w + ry[k] * vol + j + rowS) : zero;
-          wz[k] = hz[1] ? w[rz[k] * vol + j + 2] : 0.f;
-        }
-        pair_pstep(P, j, x - 1, y, z0, wj, vj, wx, wy, wz, unused, px);
-      }
-      if (ly) {  // y predecessor: its y successor is this pixel
-        const size_t j = i - rowS;
-        float2 wj[6], vj[3], wx[3], wy[3], unused[3];
-        float wz[3];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) wj[k] = ld2(w + k * vol + j);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          vj[k] = ld2(P.v + k * vol + j);
-          wx[k] = hx ? ld2(w + rx[k] * vol + j + S) : zero;
-          wy[k] = wo[ry[k]];
-          wz[k] = hz[1] ? w[rz[k] * vol + j + 2] : 0.f;
-        }
-        pair_pstep(P, j, x, y - 1, z0, wj, vj, wx, wy, wz, unused, py);
-      }
-      if (lz[0]) {  // slice z0 - 1: its z successor is the pair's first slice
-        const size_t j = i - 1;
-        float wj[6], vj[3], wx[3], wy[3], wz[3];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) wj[k] = w[k * vol + j];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          vj[k] = P.v[k * vol + j];
-          wx[k] = hx ? w[rx[k] * vol + j + S] : 0.f;
-          wy[k] = hy ? w[ry[k] * vol + j + rowS] : 0.f;
-          wz[k] = wo[rz[k]].x;
-        }
-        slice_pstep(P, j, x, y, z0 - 1, wj, vj, wx, wy, wz, pzm);
-      }
-    }
-  }
-
+  const bool hz[2] = {true, z0 + 1 < P.d.Nz - 1}, lz[2] = {z0 > 0, true};
   const float sigma = P.sigma;
-  float vv[2][K], ww[2][KW];
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const float uc = h ? u0.y : u0.x, uxn = h ? ux.y : ux.x, uyn = h ? uy.y : uy.x;
@@ -866,7 +735,8 @@ __global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
     float g[3];
     g[0] = hx ? mu + uxn : 0.f;
     g[1] = hy ? mu + uyn : 0.f;
-    g[2] = (hz[h] ? mu + uzn : 0.f) / P.stepsize;
+    g[2] = hz[h] ? mu + uzn : 0.f;
+    if (!STEP1) g[2] /= P.stepsize;
     float pc[3];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -879,7 +749,8 @@ __global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
       for (int k = 0; k < K; ++k) {
         a[k] = lx ? pc[k] - (h ? px[k].y : px[k].x) : 0.f;
         b[k] = ly ? pc[k] - (h ? py[k].y : py[k].x) : 0.f;
-        cz[k] = (lz[h] ? pc[k] - (h ? p0[k].x : pzm[k]) : 0.f) / P.stepsize;
+        cz[k] = lz[h] ? pc[k] - (h ? p0[k].x : pzm[k]) : 0.f;
+        if (!STEP1) cz[k] /= P.stepsize;
       }
       float e[6];
       e[0] = a[0]; e[1] = b[1]; e[2] = cz[2];
@@ -910,7 +781,7 @@ __global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
         }
       }
     } else {
-      const int nC = d.C;
+      const int nC = P.d.C;
       float sq[K];
 #pragma unroll
       for (int k = 0; k < K; ++k) sq[k] = vv[h][k] * vv[h][k];
@@ -944,19 +815,256 @@ __global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
       }
     }
   }
+}
 
-  if (own) {
-    float *vout = FUSED ? P.v2 : P.v, *wout = FUSED ? P.w2 : P.w;
+// k_dual_cl2: k_dual_cl for two consecutive slices z0, z0 + 1 of one channel per
+// thread (3-D, Nz even): the fields of both slices move as one float2, the slice
+// neighbours outside the pair as one float each.  Per slice the arithmetic and the
+// shuffle order are k_dual_cl's, so the iterates are bit-identical to k_dual's.
+template <bool TGV, int CPL, int CP, bool STEP1 = false>
+__global__ void __launch_bounds__(256) k_dual_cl2(const IterParams P) {
+  constexpr int K = 3, KW = 6;
+  const Dims d = P.d;
+  const int nz2 = d.Nz >> 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long vt = t / CP;  // (pixel, slice pair)
+  const int c = (int)(t - vt * CP);
+  const bool valid = vt < (long long)d.N * d.N * nz2;
+  const bool own = valid && c < d.C;
+  const int pix = valid ? (int)(vt / nz2) : 0;
+  const int z0 = valid ? 2 * (int)(vt - (long long)pix * nz2) : 0;
+  const int y = pix / d.N, x = pix - y * d.N;
+  const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
+  const bool hx = x < d.N - 1, hy = y < d.N - 1;
+  const bool lx = x > 0, ly = y > 0;
+  const float *__restrict__ ub = P.ubar;
+  const float *__restrict__ pb = P.pbar;
+  const size_t i = (size_t)pix * S + (size_t)c * d.Nz + z0;
+  const unsigned lane0 = (threadIdx.x & 31) & ~(unsigned)(CP - 1);
+
+  float2 u0 = make_float2(0.f, 0.f), ux = u0, uy = u0;
+  float uz1 = 0.f;  // ubar at z0 + 2
+  float2 p0[K], px[K], py[K], vo[K], wo[KW];
+  float pzm[K];  // pbar at z0 - 1
 #pragma unroll
-    for (int k = 0; k < K; ++k) st2(vout + k * vol + i, vv[0][k], vv[1][k]);
+  for (int k = 0; k < K; ++k) { p0[k] = px[k] = py[k] = vo[k] = u0; pzm[k] = 0.f; }
+#pragma unroll
+  for (int k = 0; k < KW; ++k) wo[k] = u0;
+  if (own) {
+    u0 = ld2(ub + i);
+    if (hx) ux = ld2(ub + i + S);
+    if (hy) uy = ld2(ub + i + rowS);
+    if (z0 + 1 < d.Nz - 1) uz1 = ub[i + 2];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      vo[k] = ld2(P.v + k * vol + i);
+      if (TGV) {
+        p0[k] = ld2(pb + k * vol + i);
+        if (lx) px[k] = ld2(pb + k * vol + i - S);
+        if (ly) py[k] = ld2(pb + k * vol + i - rowS);
+        if (z0 > 0) pzm[k] = pb[k * vol + i - 1];
+      }
+    }
     if (TGV) {
 #pragma unroll
-      for (int k = 0; k < KW; ++k) st2(wout + k * vol + i, ww[0][k], ww[1][k]);
+      for (int k = 0; k < KW; ++k) wo[k] = ld2(P.w + k * vol + i);
     }
-    if (FUSED) {
+  }
+
+  float vv[2][K], ww[2][KW];
+  dual_pair_math<TGV, CPL, CP, STEP1>(P, lane0, u0, ux, uy, uz1, p0, px, py, pzm, vo, wo, hx, hy, lx, ly, z0, vv,
+                                      ww);
+
+  if (own) {
 #pragma unroll
-      for (int k = 0; k < K; ++k) st2(P.p2 + k * vol + i, pn[k].x, pn[k].y);
+    for (int k = 0; k < K; ++k) st2(P.v + k * vol + i, vv[0][k], vv[1][k]);
+    if (TGV) {
+#pragma unroll
+      for (int k = 0; k < KW; ++k) st2(P.w + k * vol + i, ww[0][k], ww[1][k]);
     }
+  }
+}
+
+// k_dual_walk: the dual update of schedule 2 with the p / pbar half of the previous
+// iteration's primal update fused in (3-D TGV, Frobenius or uncorrelated coupling,
+// Nz even).  p, v, w are read from P.p, P.v, P.w and the new p, v, w written to
+// P.p2, P.v2, P.w2 (another buffer set: the neighbours' old values must stay while
+// other blocks read them); the pbar buffer is not used.
+//
+// The dual update at a voxel needs pbar there and at its x, y and z predecessors.
+// A block covers NCOL pixel columns (the first a halo that only computes pbar)
+// times ZC + 1 slice pairs of every channel (the first pair a halo likewise), and
+// walks down R rows from y0, with a first step at row y0 - 1 for pbar only.  Per
+// row each thread computes pbar of its own pair (update_p through pair_pstep) and
+// publishes it in shared memory: the x predecessor's pbar comes from the column to
+// the left, the z predecessor's from the pair below, the y predecessor's is the
+// thread's own pbar of the previous row (registers).  A row's operands (w, v, p,
+// the w rows and ubar of the next row, and at the block's last column / pair the
+// operands beyond it) are copied into shared memory by cp.async one row ahead, so
+// the next row's loads are in flight while a row is computed; the neighbours' w
+// rows and ubar are read from those copies.  So every field is read from HBM about
+// once, plus the halo column and pair.
+// Thread layout: t = (column * (ZC + 1) + pair) * CP + channel lane, so the CP
+// lanes of a voxel are adjacent (the coupling's shuffles).  Every value is
+// computed by the same operations as k_update and k_dual_cl2: identical iterates.
+namespace walk {
+// float2 slots of a row buffer, each [T]: w0..w5, v0..v2, p0..p2, rows (w3 w1 w5)
+// of the next row, ubar, ubar of the next row, rows (w0 w3 w4) and ubar of the x
+// successor (last column), then float slots: rows (w4 w5 w2) and ubar at slice
+// z0 + 2 (last pair)
+constexpr int W = 0, V = 6, PO = 9, WY = 12, U0 = 15, UY = 16, WXE = 17, UXE = 20, NF2 = 21;
+constexpr int WZE = 0, UZE = 3, NF1 = 4;
+constexpr size_t bytes_per_thread = 2 * (NF2 * 8 + NF1 * 4) + 3 * 8;  // two row buffers + pbar exchange
+}  // namespace walk
+
+__device__ __forceinline__ void cp_async8(void *dst, const float *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const float *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int CPL, int CP>
+__global__ void __launch_bounds__(512, 1) k_dual_walk(const IterParams P, int ZC, int NCOL, int R) {
+  using namespace walk;
+  constexpr int K = 3, KW = 6;
+  extern __shared__ float smem[];
+  const Dims d = P.d;
+  const int T = blockDim.x;
+  const int colT = (ZC + 1) * CP;
+  const int t = threadIdx.x;
+  const int col = t / colT, rr = t - col * colT;
+  const int pl = rr / CP, c = rr - pl * CP;
+  const int x = (int)blockIdx.x * (NCOL - 1) - 1 + col;
+  const int z0 = (int)blockIdx.z * 2 * ZC + 2 * (pl - 1);
+  const int y0 = (int)blockIdx.y * R;
+  const bool pthr = col < NCOL && x >= 0 && x < d.N && z0 >= 0 && z0 < d.Nz && c < d.C;
+  const bool dthr = pthr && col >= 1 && pl >= 1;
+  const bool nbx = col + 1 < NCOL;  // the x successor is in the block
+  const bool nbz = pl < ZC;         // the pair above is in the block
+  const size_t vol = d.vol, S = d.S, rowS = (size_t)d.N * S;
+  const bool hx = x < d.N - 1, lx = x > 0, hz1 = z0 + 1 < d.Nz - 1;
+  const unsigned lane0 = (threadIdx.x & 31) & ~(unsigned)(CP - 1);
+  const int rx[3] = {0, 3, 4}, ry[3] = {3, 1, 5}, rz[3] = {4, 5, 2};
+  const float *__restrict__ ub = P.ubar;
+  const float *__restrict__ w = P.w;
+  const float2 zero = make_float2(0.f, 0.f);
+  float2 *const f2base = reinterpret_cast<float2 *>(smem);                // [2][NF2][T]
+  float *const f1base = reinterpret_cast<float *>(f2base + 2 * NF2 * T);  // [2][NF1][T]
+  float2 *const spb = reinterpret_cast<float2 *>(f1base + 2 * NF1 * T);   // [3][T]
+
+  // copies of row y's operands into buffer b (threads that compute there)
+  auto issue = [&](int y, int b) {
+    if (pthr && y >= 0 && y < d.N) {
+      const size_t i = ((size_t)y * d.N + x) * S + (size_t)c * d.Nz + z0;
+      float2 *f2 = f2base + b * NF2 * T;
+      float *f1 = f1base + b * NF1 * T;
+#pragma unroll
+      for (int k = 0; k < KW; ++k) cp_async8(f2 + (W + k) * T + t, w + k * vol + i);
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        cp_async8(f2 + (V + k) * T + t, P.v + k * vol + i);
+        cp_async8(f2 + (PO + k) * T + t, P.p + k * vol + i);
+        if (y < d.N - 1) cp_async8(f2 + (WY + k) * T + t, w + ry[k] * vol + i + rowS);
+      }
+      if (dthr) {
+        cp_async8(f2 + U0 * T + t, ub + i);
+        if (y < d.N - 1) cp_async8(f2 + UY * T + t, ub + i + rowS);
+      }
+      if (!nbx && hx) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) cp_async8(f2 + (WXE + k) * T + t, w + rx[k] * vol + i + S);
+        if (dthr) cp_async8(f2 + UXE * T + t, ub + i + S);
+      }
+      if (!nbz && hz1) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) cp_async4(f1 + (WZE + k) * T + t, w + rz[k] * vol + i + 2);
+        if (dthr) cp_async4(f1 + UZE * T + t, ub + i + 2);
+      }
+    }
+    cp_async_commit();
+  };
+
+  float2 pprev[K];  // pbar of the previous row
+#pragma unroll
+  for (int k = 0; k < K; ++k) pprev[k] = zero;
+  issue(y0 - 1, 0);
+  for (int s = 0; s <= R; ++s) {
+    const int y = y0 - 1 + s;
+    const int b = s & 1;
+    const bool act = pthr && y >= 0 && y < d.N;
+    const bool hy = y < d.N - 1, ly = y > 0;
+    if (s < R) {
+      issue(y + 1, b ^ 1);
+      cp_async_wait<1>();  // this row's copies (the next row's stay in flight)
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const float2 *f2 = f2base + b * NF2 * T;
+    const float *f1 = f1base + b * NF1 * T;
+    float2 wo[KW], vo[K], po[K], wy[K], pn[K], pbr[K];
+#pragma unroll
+    for (int k = 0; k < KW; ++k) wo[k] = zero;
+#pragma unroll
+    for (int k = 0; k < K; ++k) vo[k] = po[k] = wy[k] = pn[k] = pbr[k] = zero;
+    if (act) {
+#pragma unroll
+      for (int k = 0; k < KW; ++k) wo[k] = f2[(W + k) * T + t];
+      float2 wx[K];
+      float wz[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        vo[k] = f2[(V + k) * T + t];
+        po[k] = f2[(PO + k) * T + t];
+        if (hy) wy[k] = f2[(WY + k) * T + t];
+        wx[k] = !hx ? zero : (nbx ? f2[(W + rx[k]) * T + t + colT] : f2[(WXE + k) * T + t]);
+        wz[k] = !hz1 ? 0.f : (nbz ? f2[(W + rz[k]) * T + t + CP].x : f1[(WZE + k) * T + t]);
+      }
+      pair_pstep(P, x, y, z0, po, wo, vo, wx, wy, wz, pn, pbr);
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) spb[k * T + t] = pbr[k];
+    __syncthreads();
+    if (s >= 1) {  // the dual update of row y (uniform over the block: every lane shuffles)
+      const bool dact = dthr && act;
+      float2 u0 = zero, ux = zero, uy = zero, px[K], pyv[K];
+      float uz1 = 0.f, pzm[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) { px[k] = pyv[k] = zero; pzm[k] = 0.f; }
+      if (dact) {
+        u0 = f2[U0 * T + t];
+        if (hx) ux = nbx ? f2[U0 * T + t + colT] : f2[UXE * T + t];
+        if (hy) uy = f2[UY * T + t];
+        if (hz1) uz1 = nbz ? f2[U0 * T + t + CP].x : f1[UZE * T + t];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          px[k] = spb[k * T + t - colT];
+          pyv[k] = pprev[k];
+          pzm[k] = spb[k * T + t - CP].y;
+        }
+      }
+      float vv[2][K], ww[2][KW];
+      dual_pair_math<true, CPL, CP>(P, lane0, u0, ux, uy, uz1, pbr, px, pyv, pzm, vo, wo, hx, hy, lx, ly, z0, vv,
+                                    ww);
+      if (dact) {
+        const size_t i = ((size_t)y * d.N + x) * S + (size_t)c * d.Nz + z0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) st2(P.v2 + k * vol + i, vv[0][k], vv[1][k]);
+#pragma unroll
+        for (int k = 0; k < KW; ++k) st2(P.w2 + k * vol + i, ww[0][k], ww[1][k]);
+#pragma unroll
+        for (int k = 0; k < K; ++k) st2(P.p2 + k * vol + i, pn[k].x, pn[k].y);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) pprev[k] = pbr[k];
+    __syncthreads();  // the row buffer and the pbar exchange are free for the next row
   }
 }
 
@@ -2721,9 +2829,10 @@ static cudaError_t launch_dual_c(const IterParams &P, cudaStream_t st) {
     constexpr int Q = CPL == NUCL ? FROB : CPL;
     const long long cp = C <= 1 ? 1 : (C <= 2 ? 2 : 4);
     const unsigned gc = blocks_for((long long)P.d.N * P.d.N * (P.d.Nz / 2) * cp, 128);
-    if (cp == 1) k_dual_cl2<TGV, Q, 1><<<gc, 128, 0, st>>>(P);
-    else if (cp == 2) k_dual_cl2<TGV, Q, 2><<<gc, 128, 0, st>>>(P);
-    else k_dual_cl2<TGV, Q, 4><<<gc, 128, 0, st>>>(P);
+    const bool one = P.stepsize == 1.0f;  // the divisions by the step size are left out
+    if (cp == 1) one ? k_dual_cl2<TGV, Q, 1, true><<<gc, 128, 0, st>>>(P) : k_dual_cl2<TGV, Q, 1><<<gc, 128, 0, st>>>(P);
+    else if (cp == 2) one ? k_dual_cl2<TGV, Q, 2, true><<<gc, 128, 0, st>>>(P) : k_dual_cl2<TGV, Q, 2><<<gc, 128, 0, st>>>(P);
+    else one ? k_dual_cl2<TGV, Q, 4, true><<<gc, 128, 0, st>>>(P) : k_dual_cl2<TGV, Q, 4><<<gc, 128, 0, st>>>(P);
     return cudaGetLastError();
   }
   if (P.dual_cfg >= 6 && C <= 4 && CPL != NUCL) {  // one thread per voxel-channel
@@ -2778,19 +2887,59 @@ cudaError_t launch_dual(const IterParams &P, int tgv, int cpl, cudaStream_t st) 
 // uncorrelated coupling, C <= 4, Nz even
 bool dual_fused_ok(const IterParams &P, int tgv, int cpl) { return tgv && dual_cl2_ok(P, cpl); }
 
+// k_dual_walk geometry: channel lanes CP, pairs per z-chunk ZC (at most 15, the
+// chunks as even as possible), columns per block NCOL (at most 512 threads), rows
+// per block R
+struct WalkShape {
+  int cp, zc, ncol, rows, nch, threads;
+  size_t smem;
+};
+
+static WalkShape walk_shape(const Dims &d) {
+  WalkShape w;
+  w.cp = d.C <= 1 ? 1 : (d.C <= 2 ? 2 : 4);
+  const int nz2 = d.Nz / 2;
+  w.nch = (nz2 + 14) / 15;
+  w.zc = (nz2 + w.nch - 1) / w.nch;
+  const int colT = (w.zc + 1) * w.cp;
+  w.ncol = 512 / colT;
+  w.rows = 32;
+  w.threads = (w.ncol * colT + 31) / 32 * 32;
+  w.smem = walk::bytes_per_thread * (size_t)w.threads;
+  return w;
+}
+
+template <int CPL, int CP>
+static cudaError_t walk_attr(size_t smem) {
+  return cudaFuncSetAttribute(k_dual_walk<CPL, CP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+// the shared-memory limit of the fused kernel (outside stream capture)
+cudaError_t prepare_dual_fused(const IterParams &P, int cpl) {
+  const WalkShape ws = walk_shape(P.d);
+  if (cpl == UNCORR) {
+    if (ws.cp == 1) return walk_attr<UNCORR, 1>(ws.smem);
+    if (ws.cp == 2) return walk_attr<UNCORR, 2>(ws.smem);
+    return walk_attr<UNCORR, 4>(ws.smem);
+  }
+  if (ws.cp == 1) return walk_attr<FROB, 1>(ws.smem);
+  if (ws.cp == 2) return walk_attr<FROB, 2>(ws.smem);
+  return walk_attr<FROB, 4>(ws.smem);
+}
+
 cudaError_t launch_dual_fused(const IterParams &P, int tgv, int cpl, cudaStream_t st) {
   if (!dual_fused_ok(P, tgv, cpl) || !P.p2 || !P.v2 || !P.w2) return cudaErrorInvalidValue;
-  const int C = P.d.C;
-  const int cp = C <= 1 ? 1 : (C <= 2 ? 2 : 4);
-  const unsigned g = blocks_for((long long)P.d.N * P.d.N * (P.d.Nz / 2) * cp, 128);
+  const WalkShape ws = walk_shape(P.d);
+  const dim3 grid((P.d.N + ws.ncol - 2) / (ws.ncol - 1), (P.d.N + ws.rows - 1) / ws.rows, ws.nch);
+  const unsigned nt = ws.threads;
   if (cpl == UNCORR) {
-    if (cp == 1) k_dual_cl2<true, UNCORR, 1, true><<<g, 128, 0, st>>>(P);
-    else if (cp == 2) k_dual_cl2<true, UNCORR, 2, true><<<g, 128, 0, st>>>(P);
-    else k_dual_cl2<true, UNCORR, 4, true><<<g, 128, 0, st>>>(P);
+    if (ws.cp == 1) k_dual_walk<UNCORR, 1><<<grid, nt, ws.smem, st>>>(P, ws.zc, ws.ncol, ws.rows);
+    else if (ws.cp == 2) k_dual_walk<UNCORR, 2><<<grid, nt, ws.smem, st>>>(P, ws.zc, ws.ncol, ws.rows);
+    else k_dual_walk<UNCORR, 4><<<grid, nt, ws.smem, st>>>(P, ws.zc, ws.ncol, ws.rows);
   } else {
-    if (cp == 1) k_dual_cl2<true, FROB, 1, true><<<g, 128, 0, st>>>(P);
-    else if (cp == 2) k_dual_cl2<true, FROB, 2, true><<<g, 128, 0, st>>>(P);
-    else k_dual_cl2<true, FROB, 4, true><<<g, 128, 0, st>>>(P);
+    if (ws.cp == 1) k_dual_walk<FROB, 1><<<grid, nt, ws.smem, st>>>(P, ws.zc, ws.ncol, ws.rows);
+    else if (ws.cp == 2) k_dual_walk<FROB, 2><<<grid, nt, ws.smem, st>>>(P, ws.zc, ws.ncol, ws.rows);
+    else k_dual_walk<FROB, 4><<<grid, nt, ws.smem, st>>>(P, ws.zc, ws.ncol, ws.rows);
   }
   return cudaGetLastError();
 }

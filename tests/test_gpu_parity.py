@@ -245,13 +245,15 @@ def test_projector_launch_shapes_give_identical_iterates(S_case):
                 np.testing.assert_array_equal(got[k], ref[k], err_msg=f"fwd {fc} bp {bc} field {k}")
 
 
+@pytest.mark.parametrize("stepsize", [2.0, 1.0])
 @pytest.mark.parametrize("dim,C,cpl,reg", [(3, 1, "FROB", "TGV"), (3, 2, "FROB", "TGV"), (3, 3, "UNCORR", "TGV"),
                                            (3, 4, "FROB", "TGV"), (3, 3, "FROB", "TGV"), (3, 2, "NUCL", "TGV"),
                                            (3, 4, "FROB", "TV"), (2, 4, "FROB", "TGV"), (2, 2, "NUCL", "TGV")])
-def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg):
+def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg, stepsize):
     """The two-slice float2 dual kernel, the register-capped one and the kernels that
     load every operand before the arithmetic compute every value with the same
-    operations as the one-slice kernel: identical iterates."""
+    operations as the one-slice kernel: identical iterates (step size 1: shape 9
+    leaves out the divisions by it, x / 1 = x)."""
     from graptor_gb300 import phantom
     from graptor_gb300.solver import Problem
     N, Nz, nang = 28, 6, 15
@@ -268,7 +270,7 @@ def test_dual_launch_shapes_give_identical_iterates(dim, C, cpl, reg):
         shapes = (0, 1, 2, 3, 4, 5, 6, 7, 8, 9) if z2 else (0, 2, 3, 4, 5, 6, 7, 8, 9)
     fields = ("u", "ubar", "v", "w", "p", "pbar", "lambda") if reg == "TGV" else ("u", "ubar", "v", "lambda")
     with Problem(dim, N, Nz, C, N, ang, (4, 1), [0.3] * C, regularisation=reg, coupling=cpl, normest=17.0,
-                 stepsize=2.0) as p:
+                 stepsize=stepsize) as p:
         for shape in shapes:
             # the primal update as one launch after the projectors (schedule 0), as its
             # p / pbar half beside them (schedule 1) or inside the next dual kernel

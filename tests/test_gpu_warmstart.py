@@ -52,3 +52,36 @@ def test_warm_start_with_batch_is_three_times_faster_in_wall_time():
     assert all(w is not None for w in r["warm_iterations"]), r
     assert not any(r["fell_back_to_cold"]), r
     assert r["ratio"] >= 3.0, r
+
+
+def test_warm_started_iterations_keep_fp64_parity():
+    """From the warm-started state (the committed network's u with ubar = u, lambda
+    from K u, the missed-ray lift), the device iteration tracks the FP64
+    restatement of the same iteration (oracle/fp64.py) started from that state:
+    after 300 iterations the relative L2 error of u, v and lambda is <= 1e-4, the
+    bound of the cold-start FP64 parity tests, so the warm start keeps the
+    solver's parity."""
+    import numpy as np
+
+    from graptor_gb300 import warmstart as W
+    from graptor_gb300.solver import Problem
+    from oracle import fp64 as F
+    net = W.UNet3D.load(WEIGHTS)
+    N, Nz, C, iters = 32, 8, 2, 300
+    f, ang = W.phantom_case(9060, N, Nz, C, nang=31)
+    spec = W.problem_spec(N, Nz, C, ang)
+    fields = ("u", "ubar", "p", "pbar", "v", "w", "lambda")
+    with Problem(**spec, normest=15.0) as p:
+        p.set_data(f, feasible=False)
+        W.WarmStarter(net, fields=("u",), pre_iters=50).apply(p, f)
+        st = {k: p.get(k).astype(np.float64) for k in fields}
+        p.run(iters).synchronize()
+        got = {k: p.get(k).astype(np.float64) for k in ("u", "v", "lambda")}
+    o = F.Solver64(3, N, Nz, C, N, ang, f, spec["alpha"], spec["mu"], 15.0, "KL", "TGV", "FROB", feasible=False)
+    o.u, o.ubar, o.p, o.pbar, o.v, o.w, o.lam = (st[k] for k in fields)
+    o.run(iters)
+    want = {"u": o.u, "v": o.v, "lambda": o.lam}
+    errs = {k: float(np.linalg.norm(got[k] - want[k]) / np.linalg.norm(want[k])) for k in got}
+    print({k: f"{v:.2e}" for k, v in errs.items()})
+    for k, e in errs.items():
+        assert e <= 1e-4, (k, errs)
