@@ -408,7 +408,9 @@ int autotune(gt_problem *p) {
     if (it != g_tune.end()) {
       int sched = 0;
       std::tie(p->P.fwd_cfg, p->P.bp_cfg, p->P.dual_cfg, sched) = it->second;
-      if (!p->schedule_set) p->schedule = sched;
+      // sched < 0: the schedule was chosen by gt_set_schedule when the shapes were
+      // tuned, not timed; 0 is the measured choice at 8M voxel-channels and above
+      if (!p->schedule_set) p->schedule = sched >= 0 ? sched : (p->d.vol >= (8u << 20) ? 0 : 1);
       if (p->schedule == 2 && ensure_fused(p) != GT_OK) p->schedule = 0;  // no room for the second set
       return GT_OK;
     }
@@ -513,7 +515,7 @@ int autotune(gt_problem *p) {
   cudaEventDestroy(e1);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune[key] = std::make_tuple(best[0], best[1], best[2], p->schedule);
+  g_tune[key] = std::make_tuple(best[0], best[1], best[2], p->schedule_set ? -1 : p->schedule);
   return GT_OK;
 }
 
