@@ -34,6 +34,7 @@ cudaError_t launch_radon(const float *img, float *sino, const float4 *ofs, int N
 cudaError_t launch_radon_ad(const float *sino, float *img, const float4 *ofs, int N, int nd, int nang, int S,
                             cudaStream_t st);
 cudaError_t launch_transpose(const float *in, float *out, int rows, int cols, cudaStream_t st);
+cudaError_t launch_output_f64(const float *in, double *out, int A, int B, int C, int Nz, int mode, cudaStream_t st);
 cudaError_t launch_feasible(float *f, const float *r1, int nbin1, int S, cudaStream_t st);
 cudaError_t launch_lambda_fixed(float *lam, const float *ku, const float *f, const double *mu, long long nbin, int S,
                                 int Nz, int disc, float empty_weight, float cap, cudaStream_t st);
@@ -904,6 +905,25 @@ int gt_get_state(gt_problem *p, int field, float *host) {
     CK(cudaMemcpyAsync(host + k * X * S, p->stage, sizeof(float) * X * S, cudaMemcpyDeviceToHost, p->stream));
   }
   CK(cudaStreamSynchronize(p->stream));
+  return GT_OK;
+}
+
+int gt_get_output_f64(gt_problem *p, int field, double *host) {
+  if (!p || !host) return set_err(GT_ERR_ARG, "null argument");
+  if (p->d.dim != 3 || (field != GT_U && field != GT_KU))
+    return set_err(GT_ERR_ARG, "gt_get_output_f64: the image (GT_U) or K u (GT_KU) of a 3-D problem");
+  CK(cudaSetDevice(p->device));
+  const bool img = field == GT_U;
+  const int A = img ? p->d.N : p->d.nang, B = img ? p->d.N : p->d.nd;
+  const size_t n = (size_t)A * B * p->d.S;
+  double *tmp = nullptr;
+  CK(cudaMallocAsync(&tmp, sizeof(double) * n, p->stream));
+  cudaError_t e = gt::launch_output_f64(img ? p->u : p->ku, tmp, A, B, p->d.C, p->d.Nz, img ? 0 : 1, p->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, tmp, sizeof(double) * n, cudaMemcpyDeviceToHost, p->stream);
+  const cudaError_t ef = cudaFreeAsync(tmp, p->stream);
+  if (e == cudaSuccess) e = ef;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+  if (e != cudaSuccess) return cuda_err(e, "gt_get_output_f64", __LINE__);
   return GT_OK;
 }
 

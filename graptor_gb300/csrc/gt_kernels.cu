@@ -3544,6 +3544,43 @@ cudaError_t launch_bp_table(const float4 *ofs, int N, int nd, int nang, int2 *ta
   return cudaGetLastError();
 }
 
+// A state field in the device layout in[(a B + b) S + c Nz + z] to float64 in the
+// reference's output layout: mode 0 (the image, a = y, b = x) out[c][b][a][z]
+// (Solution [C][x][y][z]); mode 1 (the sinogram, a = angle, b = bin)
+// out[c][a][z][b] (Sinogram [C][nang][Nz][nd]).  Mode 0 runs over (a, b, s) with
+// s fastest, mode 1 over (a, s, b) with b fastest, so the float64 writes are
+// contiguous (runs of Nz, resp. B).
+__global__ void k_output_f64(const float *__restrict__ in, double *__restrict__ out, int A, int B, int C, int Nz,
+                             int mode) {
+  const long long S = (long long)C * Nz;
+  const long long n = (long long)A * B * S;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    long long a, b, s;
+    if (mode == 0) {
+      s = t % S;
+      const long long ab = t / S;
+      b = ab % B;
+      a = ab / B;
+    } else {
+      b = t % B;
+      const long long as = t / B;
+      s = as % S;
+      a = as / S;
+    }
+    const long long c = s / Nz, z = s - c * Nz;
+    const float v = __ldg(in + (a * B + b) * S + s);
+    const long long o = mode == 0 ? ((c * B + b) * A + a) * Nz + z : ((c * A + a) * Nz + z) * B + b;
+    out[o] = (double)v;
+  }
+}
+
+cudaError_t launch_output_f64(const float *in, double *out, int A, int B, int C, int Nz, int mode, cudaStream_t st) {
+  const long long n = (long long)A * B * C * Nz;
+  const unsigned g = (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16);
+  k_output_f64<<<g, 256, 0, st>>>(in, out, A, B, C, Nz, mode);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_transpose(const float *in, float *out, int rows, int cols, cudaStream_t st) {
   const long long tiles = (long long)((rows + 31) / 32) * ((cols + 31) / 32);
   k_transpose<<<(unsigned)tiles, dim3(32, 8), 0, st>>>(in, out, rows, cols);
@@ -3577,11 +3614,11 @@ cudaError_t normest64(const dvec4 *ofs, int N, int nd, int nang, int rounds, dou
   for (int r = 0; r < rounds; ++r) {
     k_sum64_partial<<<nb, 256, 0, st>>>(d_img, n, d_part);
     k_sum64_partial<<<1, 256, 0, st>>>(d_part, nb, d_part + nb);
-    if (r >= 4) {  // converged (consecutive estimates within 1e-10): stop early
+    if (r >= 4) {  // converged (consecutive sums within 1e-8, the estimate then within ~1e-10): stop early
       double s = 0.0;
       if ((e = cudaMemcpyAsync(&s, d_part + nb, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
       if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-      if (std::fabs(s - prev) <= 1e-10 * std::fabs(s)) {
+      if (std::fabs(s - prev) <= 1e-8 * std::fabs(s)) {
         *out = sqrt(s);
         return cudaSuccess;
       }

@@ -74,10 +74,8 @@ def Reconstructionapproach3d(sino, angles, Parameter, mu, maxiter, ctx, plott, S
                  regularisation, coupling, float(Stepsize), normest, _device(ctx)) as prob:
         prob.set_data(f.reshape(C * Nz, nang, nd), feasible=True)
         run_with_progress(prob, int(maxiter), start, sectionwidth, _describe(current), "Section")
-        u = prob.get("u").reshape(C, Nz, nd, nd)    # [c, z, y, x]
-        ku = prob.get("ku").reshape(C, Nz, nang, nd)
-    solution = np.transpose(u, (0, 3, 2, 1)).astype(np.float64)      # [C, x, y, z]
-    sinogram = np.transpose(ku, (0, 2, 1, 3)).astype(np.float64)     # [C, nang, Nz, nd]
+        solution = prob.output_f64("u")     # [C, x, y, z], converted and reordered on the device
+        sinogram = prob.output_f64("ku")    # [C, nang, Nz, nd]
     if progress:
         print("Progress at 100%")
         print("Iterations done for section " + _describe(current))

@@ -128,6 +128,18 @@ class Problem:
         L.check(L.lib().gt_get_state(self._h, L.FIELDS[field], _ptr(out)))
         return out
 
+    def output_f64(self, field: str) -> np.ndarray:
+        """The 3-D entry point's float64 return values, reordered on the device:
+        "u" as Solution [C, N, N, Nz] (x, y, z), "ku" as Sinogram [C, nang, Nz, nd]."""
+        if field == "u":
+            out = np.empty((self.C, self.N, self.N, self.Nz), np.float64)
+        elif field == "ku":
+            out = np.empty((self.C, self.nang, self.Nz, self.nd), np.float64)
+        else:
+            raise ValueError("output_f64: 'u' or 'ku'")
+        L.check(L.lib().gt_get_output_f64(self._h, L.FIELDS[field], _ptr(out)))
+        return out
+
     def set(self, field: str, value) -> None:
         a = np.ascontiguousarray(value, dtype=np.float32).reshape(self._shape(field))
         L.check(L.lib().gt_set_state(self._h, L.FIELDS[field], _ptr(a)))

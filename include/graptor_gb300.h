@@ -98,6 +98,11 @@ GT_API int gt_synchronize(gt_problem *p);
 /* Copy one state field to / from host memory in the layout described above.
  * GT_U after gt_run is the reference's returned Solution, GT_KU its Sinogram. */
 GT_API int gt_get_state(gt_problem *p, int field, float *host);
+/* The 3-D entry point's return values in float64, converted and reordered on the
+ * device: GT_U as Solution [C][x][y][z] and GT_KU as Sinogram [C][nang][Nz][nd]
+ * (radon_tgv_primal_dual_3d.py:1277-1318, the arrays Reconstructionapproach3d
+ * returns).  host holds C N N Nz, resp. C nang Nz nd doubles.  Host-synchronous. */
+GT_API int gt_get_output_f64(gt_problem *p, int field, double *host);
 GT_API int gt_set_state(gt_problem *p, int field, const float *host);
 
 /* Launch shapes the autotuner chose: [0] forward projector, [1] back projector

@@ -63,6 +63,7 @@ def test_null_arguments():
     assert lib.gt_run(None, 1) == L.GT_ERR_ARG
     assert lib.gt_set_data(None, None, 1) == L.GT_ERR_ARG
     assert lib.gt_get_state(None, 0, None) == L.GT_ERR_ARG
+    assert lib.gt_get_output_f64(None, 0, None) == L.GT_ERR_ARG
     lib.gt_problem_destroy(None)
     # bad-projection stages: rejected on the host before any launch
     assert lib.gt_badproj_smooth(None, 3, 40, 40, 3, None, None) == L.GT_ERR_ARG

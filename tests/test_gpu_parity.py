@@ -355,6 +355,31 @@ def test_fused_schedule_gives_the_iterates_of_plain_iterations(C, cpl, Nz):
         assert any(not np.array_equal(before[k], after[k]) for k in fields)
 
 
+def test_float64_outputs_are_the_reordered_state():
+    """gt_get_output_f64 (the drop-in entry point's return values, converted and
+    reordered on the device) equals the float32 state reordered on the host:
+    Solution [C, x, y, z] and Sinogram [C, nang, Nz, nd], value for value; other
+    fields and 2-D problems are refused."""
+    from graptor_gb300 import _lib as L
+    from graptor_gb300 import phantom
+    from graptor_gb300.solver import Problem
+    N, Nz, C, nang, nd = 20, 3, 2, 11, 23
+    rng = np.random.default_rng(77)
+    ang = phantom.angles_deg(nang)
+    f = np.abs(rng.standard_normal((C * Nz, nang, nd))).astype(np.float32)
+    with Problem(3, N, Nz, C, nd, ang, (4, 1), [0.3] * C, normest=17.0) as p:
+        p.set_data(f).run(7).synchronize()
+        u = p.get("u").reshape(C, Nz, N, N)
+        ku = p.get("ku").reshape(C, Nz, nang, nd)
+        np.testing.assert_array_equal(p.output_f64("u"), np.transpose(u, (0, 3, 2, 1)).astype(np.float64))
+        np.testing.assert_array_equal(p.output_f64("ku"), np.transpose(ku, (0, 2, 1, 3)).astype(np.float64))
+        out = np.empty(8)
+        assert L.lib().gt_get_output_f64(p._h, L.FIELDS["v"], out.ctypes.data) == L.GT_ERR_ARG
+    with Problem(2, N, 1, C, nd, ang, (4, 1), [0.3] * C, normest=17.0) as q:
+        with pytest.raises(ValueError):
+            q.output_f64("u")
+
+
 @pytest.mark.parametrize("disc", ["KL", "L2"])
 def test_dual_from_primal_is_a_fixed_point(disc):
     """lambda from gt_dual_from_primal equals the fixed point of the lambda update
