@@ -705,6 +705,8 @@ def run_gapsweep(args, rank, world, local):
     for w in [float(x) for x in args.primal_weights.split(",")]:
         with Problem(**WS.problem_spec(N, Nz, WARM["C"], ang), device=local) as p:
             p.set_data(f).set_primal_weight(w).snapshot()
+            if args.precise:
+                p.set_precise_primal()
             t0 = time.perf_counter()
             hist, done = [], 0
             while done < args.steps:
@@ -726,7 +728,7 @@ def run_gapsweep(args, rank, world, local):
             "n_gpus": world, "steps": args.steps, "warmup": 0, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 2-channel ellipsoid phantom)",
             "config": {"workload": f"primal-weight sweep: 3D TGV-KL FROB {N}x{N}x{Nz}, 2 channels, "
-                                   f"{WARM['nang']} angles, cold start"},
+                                   f"{WARM['nang']} angles, cold start", "precise_primal": bool(args.precise)},
             "sweep": rows}
 
 
@@ -889,6 +891,8 @@ def main():
                     help="--workload batched: the uneven config-3 sizes or many small problems")
     ap.add_argument("--seeds", type=int, default=8, help="held-out problems per rank for --workload warmstart")
     ap.add_argument("--primal-weights", default="1,3,10", help="--workload gapsweep: primal weights to sweep")
+    ap.add_argument("--precise", action="store_true",
+                    help="--workload gapsweep / warmstart: u held as two floats (gt_set_precise_primal)")
     ap.add_argument("--fields", default="u", help="--workload warmstart: the fields the network predicts (u or u,v)")
     ap.add_argument("--tol", type=float, default=None, help="--workload warmstart: relative gap tolerance (1e-2)")
     ap.add_argument("--ttg-seeds", type=int, default=4,

@@ -70,6 +70,8 @@ _SIGS = {
     "gt_synchronize": (ctypes.c_int, [_P]),
     "gt_get_state": (ctypes.c_int, [_P, ctypes.c_int, _P]),
     "gt_get_output_f64": (ctypes.c_int, [_P, ctypes.c_int, _P]),
+    "gt_set_precise_primal": (ctypes.c_int, [_P, ctypes.c_int]),
+    "gt_get_precise_primal": (ctypes.c_int, [_P]),
     "gt_set_state": (ctypes.c_int, [_P, ctypes.c_int, _P]),
     "gt_get_scalars": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
     "gt_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),

@@ -189,6 +189,7 @@ struct gt_problem {
   void *gap_ws = nullptr;      // gap workspace (v~ planes + FP64 block partials), allocated on first gt_gap
   float *snap = nullptr;       // copy of (u, p, v, w, lambda) for gt_movement, allocated on first gt_snapshot
   float *fused = nullptr;      // second (p, v, w) of schedule 2, allocated when that schedule is timed or set
+  float *ulo = nullptr;        // low parts of u in the precise primal mode (gt_set_precise_primal), or null
   double pweight = 1.0;        // primal weight: sigma = w / sqrt(Lsqr), tau = 1 / (w sqrt(Lsqr)); 1 = reference
   double *mu64 = nullptr;
   gt::IterParams P{};
@@ -786,6 +787,7 @@ void gt_problem_destroy(gt_problem *p) {
   if (p->gap_ws) cudaFree(p->gap_ws);
   if (p->snap) cudaFree(p->snap);
   if (p->fused) cudaFree(p->fused);
+  if (p->ulo) cudaFree(p->ulo);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
   if (p->side) cudaStreamDestroy(p->side);
@@ -842,6 +844,7 @@ int gt_set_data(gt_problem *p, const float *f_host, int make_feasible) {
   const size_t fv = sizeof(float) * d.vol;
   CK(cudaMemsetAsync(p->u, 0, fv, p->stream));
   CK(cudaMemsetAsync(p->ubar, 0, fv, p->stream));
+  if (p->ulo) CK(cudaMemsetAsync(p->ulo, 0, fv, p->stream));
   if (p->p) CK(cudaMemsetAsync(p->p, 0, fv * p->K, p->stream));
   if (p->pbar) CK(cudaMemsetAsync(p->pbar, 0, fv * p->K, p->stream));
   CK(cudaMemsetAsync(p->v, 0, fv * p->K, p->stream));
@@ -939,6 +942,7 @@ int gt_set_state(gt_problem *p, int field, const float *host) {
     CK(cudaMemcpyAsync(p->stage, host + k * X * S, sizeof(float) * X * S, cudaMemcpyHostToDevice, p->stream));
     CK(gt::launch_transpose(p->stage, ptr + k * plane, (int)S, (int)X, p->stream));
   }
+  if (field == GT_U && p->ulo) CK(cudaMemsetAsync(p->ulo, 0, sizeof(float) * p->d.vol, p->stream));
   CK(cudaStreamSynchronize(p->stream));
   return GT_OK;
 }
@@ -968,6 +972,7 @@ int gt_set_state_device(gt_problem *p, int field, const float *dev) {
     const size_t plane = (field == GT_LAMBDA || field == GT_KU || field == GT_DATA) ? p->d.nbin : p->d.vol;
     CK(gt::launch_transpose(dev + k * X * S, ptr + k * plane, (int)S, (int)X, p->stream));
   }
+  if (field == GT_U && p->ulo) CK(cudaMemsetAsync(p->ulo, 0, sizeof(float) * p->d.vol, p->stream));
   return GT_OK;
 }
 
@@ -1033,6 +1038,31 @@ int gt_set_dual_shape(gt_problem *p, int cfg) {
 int gt_get_dual_shape(gt_problem *p) { return p ? p->P.dual_cfg : -1; }
 
 int gt_get_schedule(gt_problem *p) { return p ? p->schedule : -1; }
+
+int gt_set_precise_primal(gt_problem *p, int on) {
+  if (!p) return set_err(GT_ERR_ARG, "null argument");
+  CK(cudaSetDevice(p->device));
+  CK(cudaStreamSynchronize(p->stream));
+  if (on && !p->ulo) {
+    cudaError_t e = cudaMalloc(&p->ulo, sizeof(float) * p->d.vol);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p->ulo = nullptr;
+      return set_err(GT_ERR_OOM, "precise primal mode: allocation of %.3f GB failed", 4e-9 * p->d.vol);
+    }
+    CK(cudaMemset(p->ulo, 0, sizeof(float) * p->d.vol));  // u = u + 0: the current iterate
+  } else if (!on && p->ulo) {
+    CK(cudaFree(p->ulo));
+    p->ulo = nullptr;
+  }
+  p->P.ulo = p->ulo;
+  // the captured graphs hold the old parameters
+  if (p->g_one) { cudaGraphExecDestroy(p->g_one); p->g_one = nullptr; }
+  if (p->g_chunk) { cudaGraphExecDestroy(p->g_chunk); p->g_chunk = nullptr; }
+  return GT_OK;
+}
+
+int gt_get_precise_primal(gt_problem *p) { return p && p->ulo ? 1 : 0; }
 
 int gt_set_primal_weight(gt_problem *p, double w) {
   if (!p || !(w > 0) || !std::isfinite(w)) return set_err(GT_ERR_ARG, "primal weight must be positive and finite");

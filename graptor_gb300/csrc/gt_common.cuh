@@ -57,6 +57,7 @@ struct IterParams {
   float *lam, *f, *ku;   // [nbin]
   float *kstar;          // [vol] back projection K* lambda
   float *p2, *v2, *w2;   // outputs of k_dual_cl2's fused form (p, v, w of the next iterate), or null
+  float *ulo;            // [vol] low parts of u in the precise primal mode (u = u + ulo), or null
   const double *mu64;    // [C] mu (KL) or mu (L2) in double, for the gap
   double ne64;           // operator-norm estimate, for the gap
   const void *bp_tmap;   // host copies of the TMA descriptors of lambda for k_bp_tma with

@@ -1855,6 +1855,8 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
     ldw<UW>(v + 2 * vol + i, c);
     if (z[0] > 0) cprev = v[2 * vol + i - 1];
   }
+  float lo[UW], lon[UW];  // the low parts of u (precise primal mode, P.ulo set)
+  if (P.ulo) ldw<UW>(P.ulo + i, lo);
 #pragma unroll
   for (int k = 0; k < UW; ++k) {
     float ak = a[k], bk = b[k];
@@ -1862,22 +1864,38 @@ __device__ __forceinline__ void primal_update(const IterParams &P, int x, int y,
     if (x > 0) ak -= am[k];
     if (y == d.N - 1) bk = 0.f;
     if (y > 0) bk -= bm[k];
-    float r;
+    float sum;
     if (DIM == 3) {
       float ck = c[k];
       if (z[k] == d.Nz - 1) ck = 0.f;
       if (z[k] > 0) ck -= (k > 0 ? c[k - 1] : cprev);
       ck /= P.stepsize;
-      r = uo[k] + P.tau * (ak + bk + ck - P.norming * kstar[k]);
+      sum = ak + bk + ck - P.norming * kstar[k];
     } else {
-      r = uo[k] + P.tau * (ak + bk - P.norming * kstar[k]);
+      sum = ak + bk - P.norming * kstar[k];
     }
-    if (r < 0.f) r = 0.f;
-    un[k] = r;
-    ub[k] = 2.0f * r - uo[k];
+    if (!P.ulo) {  // the reference's update (one rounding of u + tau sum)
+      float r = uo[k] + P.tau * sum;
+      if (r < 0.f) r = 0.f;
+      un[k] = r;
+      ub[k] = 2.0f * r - uo[k];
+    } else {
+      // u held as uo + lo (two floats): the step is added to the low part and
+      // the pair renormalised by TwoSum (Knuth), so steps below half an ulp of u
+      // are kept instead of absorbed
+      const float t = lo[k] + P.tau * sum;
+      const float r = __fadd_rn(uo[k], t);
+      const float bv = __fsub_rn(r, uo[k]);
+      const float e = __fadd_rn(__fsub_rn(uo[k], __fsub_rn(r, bv)), __fsub_rn(t, bv));
+      const bool neg = r < 0.f || (r == 0.f && e < 0.f);
+      un[k] = neg ? 0.f : r;
+      lon[k] = neg ? 0.f : e;
+      ub[k] = (2.0f * un[k] - uo[k]) + (2.0f * lon[k] - lo[k]);
+    }
   }
   stv<UW>(P.ubar + i, ub);
   stv<UW>(P.u + i, un);
+  if (P.ulo) stv<UW>(P.ulo + i, lon);
   }
 
   if (TGV && PART != PART_U) {

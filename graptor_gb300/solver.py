@@ -187,6 +187,16 @@ class Problem:
         L.check(L.lib().gt_set_schedule(self._h, int(schedule)))
         return self
 
+    def set_precise_primal(self, on: bool = True):
+        """Hold u as two floats so that steps below half an ulp of u are kept (the
+        relative gap then falls below the float32 plateau; see gt_set_precise_primal)."""
+        L.check(L.lib().gt_set_precise_primal(self._h, int(bool(on))))
+        return self
+
+    @property
+    def precise_primal(self) -> bool:
+        return bool(L.lib().gt_get_precise_primal(self._h))
+
     def dual_from_primal(self, empty_weight: float = 1.0, cap: int = 0, repair: bool = False):
         """Set lambda consistent with the current u (for warm starts); bins
         without data move empty_weight of the way to their fixed point; cap 10

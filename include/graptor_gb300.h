@@ -138,6 +138,17 @@ GT_API int gt_get_dual_shape(gt_problem *p);
  * (gt_set_data) times them as graph-captured iterations and keeps the fastest,
  * unless gt_set_schedule chose one; gt_get_schedule returns the current. */
 GT_API int gt_set_schedule(gt_problem *p, int schedule);
+/* Precise primal mode (no counterpart in the reference, off by default).  The
+ * reference stores u in float32, so a primal step smaller than half an ulp of u
+ * is lost; near convergence that stalls the relative primal-dual gap at a few
+ * 1e-4 on volumes of 64^2 x 16 and more (an FP64 run of the same iteration keeps
+ * falling).  With on = 1, u is held as two floats (u and a low part, 4 more bytes
+ * per voxel-channel, allocated here and reset with the iterate): each step is
+ * added to the low part and the pair renormalised (TwoSum), ubar is rounded from
+ * the pair; everything else is unchanged.  gt_get_state returns the high part;
+ * setting u (gt_set_state, gt_set_state_device) clears the low part. */
+GT_API int gt_set_precise_primal(gt_problem *p, int on);
+GT_API int gt_get_precise_primal(gt_problem *p);
 GT_API int gt_get_schedule(gt_problem *p);
 
 /* Time-to-gap building blocks (restarted primal-dual iterations).  No

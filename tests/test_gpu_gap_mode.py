@@ -87,3 +87,32 @@ def test_restart_snapshot_and_movement():
         p.restart().synchronize()
         np.testing.assert_array_equal(p.get("ubar"), p.get("u"))
         np.testing.assert_array_equal(p.get("pbar"), p.get("p"))
+
+
+def test_precise_primal_passes_the_float32_gap_plateau():
+    """The time-to-gap workload's phantom at 48^2 x 8 x 2 (seed 9000, 71 angles),
+    primal weight 10, 40,000 iterations.  With u stored in float32, as the
+    reference does, the relative gap stalls above 2e-4: primal steps below half an
+    ulp of u are lost (the FP64 restatement with only u rounded to float32 after
+    every update stalls at 3.5e-4 as well, while with u in FP64 and every other
+    field rounded it reaches 6e-5).  With u held as two floats
+    (gt_set_precise_primal) the gap falls below 1e-4, and the iterate agrees with
+    the float32 one to the size of the difference the gap measures."""
+    from graptor_gb300 import warmstart as WS
+    from graptor_gb300.solver import Problem
+    N, Nz = 48, 8
+    f, ang = WS.phantom_case(9000, N, Nz, 2, 71)
+    gaps, us = {}, {}
+    for precise in (False, True):
+        with Problem(**WS.problem_spec(N, Nz, 2, ang)) as p:
+            p.set_data(f).set_primal_weight(10.0)
+            if precise:
+                p.set_precise_primal()
+            assert p.precise_primal == precise
+            p.run(40000).synchronize()
+            gaps[precise] = p.gap()["relative"]
+            us[precise] = p.get("u")
+    print(gaps)
+    assert gaps[True] < 1e-4, gaps
+    assert gaps[False] > 2e-4, gaps
+    assert rel(us[True], us[False]) < 1e-2
