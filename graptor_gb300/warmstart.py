@@ -461,10 +461,12 @@ def problem_spec(N, Nz, C, ang, mu=(0.2, 5e-4), alpha=(4.0, 1.0)):
 
 
 def generate_pairs(seeds, N, Nz, C=2, nang=71, mu=(0.2, 5e-4), alpha=(4.0, 1.0), fields=("u", "v"),
-                   pre_iters=20, target_iters=5000, device=0, log=None):
+                   pre_iters=20, target_iters=5000, device=0, log=None, target_pweight=1.0, target_precise=False):
     """Training pairs from the plain solver: input = u after pre_iters cold
     iterations / s_c, target = the fields after target_iters iterations,
     normalised (:func:`field_scales`).  The problems run together as one Batch.
+    After the input is taken the iterations towards the target may use another
+    primal weight and the precise primal mode (targets closer to the minimiser).
     Returns host arrays x [n][C][Nz][N][N] and y [n][cout][Nz][N][N]."""
     from .solver import Batch
     cases = [phantom_case(s, N, Nz, C, nang, device=device) for s in seeds]
@@ -483,6 +485,13 @@ def generate_pairs(seeds, N, Nz, C=2, nang=71, mu=(0.2, 5e-4), alpha=(4.0, 1.0),
             sc = channel_scales(f, C, Nz, N, len(ang))
             scs.append(sc)
             xs[k] = b[k].get("u").reshape(C, Nz, N, N) / sc[:, None, None, None]
+        if target_pweight != 1.0 or target_precise:
+            for k in range(len(cases)):
+                if target_pweight != 1.0:
+                    b[k].set_primal_weight(target_pweight)
+                if target_precise:
+                    b[k].set_precise_primal()
+            b.invalidate()
         b.run(target_iters - pre_iters).synchronize()
         for k in range(len(cases)):
             fs = field_scales(fields, scs[k], alpha, b[k].scalars["normest"])
@@ -627,6 +636,10 @@ def _main(argv=None):
     ap.add_argument("--pairs", type=int, default=64, help="training problems (seeds 1000..)")
     ap.add_argument("--target-iters", type=int, default=8000)
     ap.add_argument("--pre-iters", type=int, default=500)
+    ap.add_argument("--target-pweight", type=float, default=1.0,
+                    help="primal weight of the iterations towards the target (after the input is taken)")
+    ap.add_argument("--target-precise", action="store_true",
+                    help="the iterations towards the target hold u as two floats (gt_set_precise_primal)")
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--crop", default="16,64,64")
@@ -652,7 +665,8 @@ def _main(argv=None):
             xs, ys = [], []
             for k in range(0, len(seeds), 16):
                 x, y = generate_pairs(seeds[k:k + 16], a.N, a.Nz, a.C, a.nang, fields=gen_fields,
-                                      pre_iters=a.pre_iters, target_iters=a.target_iters, log=log)
+                                      pre_iters=a.pre_iters, target_iters=a.target_iters, log=log,
+                                      target_pweight=a.target_pweight, target_precise=a.target_precise)
                 xs.append(x)
                 ys.append(y)
             xs, ys = np.concatenate(xs), np.concatenate(ys)
