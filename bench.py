@@ -355,8 +355,8 @@ def run_ours(args, rank, world, local):
     # 128^2 x 32 x 2 with the reference's steps and float32 u
     ttg = ttg2 = None
     if args.ttg_seeds > 0:
-        ttg = time_to_gap_compare(rank, world, local, args.ttg_seeds, N=64, Nz=16, tol=1e-4, pweight=10.0,
-                                  precise=True, check_every=1000, max_iters=200000)
+        ttg = time_to_gap_compare(rank, world, local, args.ttg_seeds, weights=WARM["weights_1e4"], N=64, Nz=16,
+                                  tol=1e-4, pweight=10.0, precise=True, check_every=1000, max_iters=200000)
         ttg2 = time_to_gap_compare(rank, world, local, args.ttg_seeds)
     if rank != 0:
         return None
@@ -494,7 +494,9 @@ def run_batched(args, rank, world, local):
 
 
 WARM = dict(N=128, Nz=32, C=2, nang=71, pre=500, tol=1e-2, check_every=100, max_iters=40000, fallback_after=10000,
-            weights=os.path.join(ROOT, "graptor_gb300", "weights", "unet_tgv_kl_c2_p500.npz"))
+            weights=os.path.join(ROOT, "graptor_gb300", "weights", "unet_tgv_kl_c2_p500.npz"),
+            # trained on targets of the precise primal mode with primal weight 10 (the 1e-4 solver)
+            weights_1e4=os.path.join(ROOT, "graptor_gb300", "weights", "unet_tgv_kl_c2_p500_w10.npz"))
 
 
 def run_unet(args, rank, world, local):

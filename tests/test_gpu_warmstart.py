@@ -87,16 +87,18 @@ def test_warm_started_iterations_keep_fp64_parity():
         assert e <= 1e-4, (k, errs)
 
 
-def test_warm_start_reaches_gap_1e4_twice_as_fast_in_wall_time():
+def test_warm_start_reaches_gap_1e4_faster_in_wall_time():
     """At the metric's tolerance, relative gap 1e-4, on four held-out 64^2 x 16 x 2
     problems (seeds 9000-9003): both arms hold u as two floats and use primal
     weight 10 after the warm arm's 500 cold iterations; every problem of both arms
     reaches the tolerance within 200,000 iterations, and the learned warm start
-    with the problems in one batch takes at most half the wall time of the cold
-    start (3.2x measured)."""
+    (the network trained on targets of that solver,
+    graptor_gb300/weights/unet_tgv_kl_c2_p500_w10.npz) with the problems in one
+    batch takes at most 1/2.5 of the wall time of the cold start (3.4x measured)."""
     import bench
-    r = bench.time_to_gap_compare(0, 1, 0, 4, WEIGHTS, 64, 16, 1e-4, pweight=10.0, precise=True,
+    w10 = os.path.join(os.path.dirname(WEIGHTS), "unet_tgv_kl_c2_p500_w10.npz")
+    r = bench.time_to_gap_compare(0, 1, 0, 4, w10, 64, 16, 1e-4, pweight=10.0, precise=True,
                                   check_every=1000, max_iters=200000)
     assert all(c < 200000 for c in r["cold_iterations"]), r
     assert all(w is not None for w in r["warm_iterations"]), r
-    assert r["ratio"] >= 2.0, r
+    assert r["ratio"] >= 2.5, r
