@@ -343,7 +343,7 @@ def run_ours(args, rank, world, local):
                                            "KL", COUPLING_METHOD[W["coupling"]], "TGV", [0.0, 1.0, [0]])
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     h2d = 4 * Sb
-    d2h = 4 * V + 4 * Sb
+    d2h = 8 * V + 8 * Sb  # the float64 Solution and Sinogram the entry point returns
     e2e = {"value": world * V * args.steps / e2e_s, "unit": METRIC,
            "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
            "seconds": e2e_s, "includes": "problem setup, H2D of the sinograms, FP64 operator-norm estimate, "
