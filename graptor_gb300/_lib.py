@@ -15,7 +15,7 @@ GT_OK, GT_ERR_OOM, GT_ERR_ARG, GT_ERR_TIMEOUT, GT_ERR_CUDA, GT_ERR_STATE = range
 GT_KL, GT_L2 = 0, 1
 GT_TV, GT_TGV = 0, 1
 GT_UNCORR, GT_FROB, GT_NUCL = 0, 1, 2
-FIELDS = {"u": 0, "ubar": 1, "p": 2, "pbar": 3, "v": 4, "w": 5, "lambda": 6, "ku": 7, "data": 8}
+FIELDS = {"u": 0, "ubar": 1, "p": 2, "pbar": 3, "v": 4, "w": 5, "lambda": 6, "ku": 7, "data": 8, "ulo": 9}
 
 
 class GraptorError(RuntimeError):

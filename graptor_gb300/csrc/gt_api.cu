@@ -329,9 +329,10 @@ int field_info(gt_problem *p, int field, float **ptr, int *comps, size_t *X) {
     case GT_LAMBDA: *ptr = p->lam; *comps = 1; *X = sino; break;
     case GT_KU: *ptr = p->ku; *comps = 1; *X = sino; break;
     case GT_DATA: *ptr = p->f; *comps = 1; *X = sino; break;
+    case GT_ULO: *ptr = p->ulo; *comps = 1; *X = img; break;
     default: return set_err(GT_ERR_ARG, "unknown state field %d", field);
   }
-  if (!*ptr) return set_err(GT_ERR_ARG, "state field %d does not exist for this regularisation", field);
+  if (!*ptr) return set_err(GT_ERR_ARG, "state field %d does not exist for this problem (regularisation, mode)", field);
   return GT_OK;
 }
 

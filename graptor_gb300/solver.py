@@ -121,7 +121,7 @@ class Problem:
     def _shape(self, field):
         img, sino = (self.S, self.N, self.N), (self.S, self.nang, self.nd)
         return {"u": img, "ubar": img, "p": (self.K,) + img, "pbar": (self.K,) + img, "v": (self.K,) + img,
-                "w": (self.KW,) + img, "lambda": sino, "ku": sino, "data": sino}[field]
+                "w": (self.KW,) + img, "lambda": sino, "ku": sino, "data": sino, "ulo": img}[field]
 
     def get(self, field: str) -> np.ndarray:
         out = np.empty(self._shape(field), np.float32)
@@ -250,13 +250,15 @@ class Problem:
 
     # ------------------------------------------------------------------ checkpoint / resume
     def _state_fields(self):
-        return ("u", "ubar", "p", "pbar", "v", "w", "lambda") if self.regularisation == "TGV" else \
+        f = ("u", "ubar", "p", "pbar", "v", "w", "lambda") if self.regularisation == "TGV" else \
             ("u", "ubar", "v", "lambda")
+        return f + ("ulo",) if self.precise_primal else f  # the low part after u (setting u clears it)
 
     def save(self, path: str) -> None:
         """Checkpoint the solve to ``path`` (.npz): the problem description, the
-        data, the step-size scalars (operator-norm estimate included) and every
-        iterate, so that :meth:`load` continues the iteration exactly."""
+        data, the step-size scalars (operator-norm estimate and primal weight
+        included), the precise primal mode and every iterate (the low part of u
+        with it), so that :meth:`load` continues the iteration exactly."""
         self.synchronize()
         sc = self.scalars
         fields = {k: self.get(k) for k in self._state_fields()}
@@ -264,6 +266,7 @@ class Problem:
                  alpha=self.alpha, mu=self.mu, discrepancy=self.discrepancy, regularisation=self.regularisation,
                  coupling=self.coupling, stepsize=self.stepsize, normest=sc["normest"],
                  iterations=sc["iterations"] + getattr(self, "iteration_offset", 0), data=self.get("data"),
+                 primal_weight=self.primal_weight, precise_primal=self.precise_primal,
                  **{"state_" + k: v for k, v in fields.items()})
 
     @classmethod
@@ -275,6 +278,10 @@ class Problem:
                 z["mu"], str(z["discrepancy"]), str(z["regularisation"]), str(z["coupling"]), float(z["stepsize"]),
                 float(z["normest"]), device, stream, autotune)
         p.set_data(z["data"], feasible=False)  # stored after the feasibility mask
+        if "primal_weight" in z.files and float(z["primal_weight"]) != 1.0:
+            p.set_primal_weight(float(z["primal_weight"]))
+        if "precise_primal" in z.files and bool(z["precise_primal"]):
+            p.set_precise_primal(True)
         for k in p._state_fields():
             p.set(k, z["state_" + k])
         p.iteration_offset = int(z["iterations"])

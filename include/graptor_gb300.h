@@ -51,7 +51,8 @@ enum { GT_TV = 0, GT_TGV = 1 };              /* regularisation, :1040-1051 */
 enum { GT_UNCORR = 0, GT_FROB = 1, GT_NUCL = 2 }; /* coupling, :1079-1130 */
 
 /* state fields for gt_get_state / gt_set_state (the reference's U, U_, P, P_, V, W, Lamb) */
-enum { GT_U = 0, GT_UBAR = 1, GT_P = 2, GT_PBAR = 3, GT_V = 4, GT_W = 5, GT_LAMBDA = 6, GT_KU = 7, GT_DATA = 8 };
+enum { GT_U = 0, GT_UBAR = 1, GT_P = 2, GT_PBAR = 3, GT_V = 4, GT_W = 5, GT_LAMBDA = 6, GT_KU = 7, GT_DATA = 8,
+       GT_ULO = 9 /* low part of u in the precise primal mode (gt_set_precise_primal) */ };
 
 /* Problem description.  Mirrors the argument surface of Reconstructionapproach2d/3d
  * (radon_tgv_primal_dual_2d.py:69, radon_tgv_primal_dual_3d.py:69). */
@@ -145,8 +146,10 @@ GT_API int gt_set_schedule(gt_problem *p, int schedule);
  * falling).  With on = 1, u is held as two floats (u and a low part, 4 more bytes
  * per voxel-channel, allocated here and reset with the iterate): each step is
  * added to the low part and the pair renormalised (TwoSum), ubar is rounded from
- * the pair; everything else is unchanged.  gt_get_state returns the high part;
- * setting u (gt_set_state, gt_set_state_device) clears the low part. */
+ * the pair; everything else is unchanged.  gt_get_state(GT_U) returns the high
+ * part and GT_ULO the low part (field of the image's size; GT_ERR_ARG when the
+ * mode is off); setting u (gt_set_state, gt_set_state_device) clears the low
+ * part, so a checkpoint restores u first, then GT_ULO. */
 GT_API int gt_set_precise_primal(gt_problem *p, int on);
 GT_API int gt_get_precise_primal(gt_problem *p);
 GT_API int gt_get_schedule(gt_problem *p);

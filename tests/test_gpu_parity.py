@@ -509,10 +509,11 @@ def test_out_of_memory_is_a_memory_error():
         p.set_data(np.ones((2, 30, 16), np.float32)).run(2).synchronize()
 
 
-@pytest.mark.parametrize("reg", ["TGV", "TV"])
-def test_checkpoint_resume_continues_exactly(tmp_path, reg):
+@pytest.mark.parametrize("reg,mode", [("TGV", "plain"), ("TV", "plain"), ("TGV", "precise")])
+def test_checkpoint_resume_continues_exactly(tmp_path, reg, mode):
     """save() after 20 iterations, load() into a new problem: its next 10 iterations
-    equal those of the saved problem, bit for bit."""
+    equal those of the saved problem, bit for bit (with primal weight 7 and the
+    precise primal mode: both restored, the low part of u included)."""
     from graptor_gb300 import phantom
     from graptor_gb300.solver import Problem
     rng = np.random.default_rng(91)
@@ -521,12 +522,22 @@ def test_checkpoint_resume_continues_exactly(tmp_path, reg):
     f = np.abs(rng.standard_normal((C * Nz, nang, N))).astype(np.float32)
     path = str(tmp_path / "ckpt.npz")
     with Problem(3, N, Nz, C, N, ang, (4, 1), [0.2, 0.05], regularisation=reg) as p:
-        p.set_data(f).run(20)
+        p.set_data(f)
+        if mode == "precise":
+            p.set_primal_weight(7.0).set_precise_primal()
+        p.run(20)
         p.save(path)
         p.run(10).synchronize()
         want = {k: p.get(k) for k in p._state_fields()}
+        if mode == "precise":
+            assert "ulo" in want and np.abs(want["ulo"]).max() > 0
+        else:
+            with pytest.raises(ValueError):
+                p.get("ulo")
     with Problem.load(path) as q:
         assert q.iteration_offset == 20
+        assert q.precise_primal == (mode == "precise")
+        assert q.primal_weight == (7.0 if mode == "precise" else 1.0)
         q.run(10).synchronize()
         for k, v in want.items():
             np.testing.assert_array_equal(q.get(k), v, err_msg=k)
